@@ -1,0 +1,215 @@
+/*
+ * topt.h -- C ABI of libtopt_gb300, the GB300 (sm_103a) engine behind the
+ * scikit-topt density-method hot path.
+ *
+ * Every entry point takes plain pointers and sizes.  Device pointers are
+ * marked "dev"; everything else is host memory.  Functions return a status
+ * code (TOPT_OK on success); topt_last_error() gives the message of the most
+ * recent failure on the calling thread.  Work is issued on the stream set on
+ * the handle (default stream when none was set) and is stream-ordered; a
+ * handle is not thread-safe.
+ *
+ * Each declaration names the reference interface it replaces (paths relative
+ * to the scikit-topt project root).  The reference is a Python library whose
+ * plugin objects (FEM, filter, rho_update) are duck-typed; these functions are
+ * what those objects call through ctypes.
+ */
+#ifndef TOPT_GB300_H
+#define TOPT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define TOPT_OK 0
+#define TOPT_MAXITER 1      /* an iterative method stopped at its cap      */
+#define TOPT_NONFINITE 2    /* NaN/Inf met in a residual or reduction      */
+#define TOPT_BREAKDOWN 3    /* CG breakdown (p.Ap <= 0)                     */
+#define TOPT_BAD_INPUT 4    /* invalid argument, size or index             */
+#define TOPT_CUDA_ERROR 5   /* a CUDA runtime call failed                   */
+#define TOPT_NO_MEMORY 6    /* device or host allocation failed            */
+
+/* value types */
+#define TOPT_F64 0
+#define TOPT_F32 1
+
+const char* topt_version(void);
+const char* topt_last_error(void);
+/* Number of kernels this library has launched in the process (counted on the
+ * device by every launch; synchronises with the device). */
+int topt_launch_count(uint64_t* out);
+
+/* ------------------------------------------------------------------------
+ * Sparsity pattern (host only, no GPU).
+ * Replaces the COO->CSR conversion of scikit-fem ``asm`` + ``.tocsr()``
+ * (sktopt/fea/composer.py:80-100, sktopt/fea/solver_elastic.py:205).
+ * Nodes i, j are coupled when they share an element; columns are sorted.
+ * The scalar CSR with interleaved DOFs bs*node+comp is the bs x bs block
+ * expansion of this node pattern.  contrib lists, per block, the element
+ * contributions e*nloc*nloc + la*nloc + lb in ascending element order.
+ * ---------------------------------------------------------------------- */
+typedef struct topt_pattern topt_pattern;
+int topt_pattern_build(int64_t n_nodes, int64_t n_elem, int32_t nloc,
+                       const int32_t* t /* (nloc, n_elem) row-major */,
+                       topt_pattern** out);
+int topt_pattern_sizes(const topt_pattern* p, int64_t* nnzb, int64_t* ncontrib);
+int topt_pattern_export(const topt_pattern* p, int32_t* rowptr /* n_nodes+1 */,
+                        int32_t* colind /* nnzb */, int64_t* cptr /* nnzb+1 */,
+                        int32_t* contrib /* ncontrib */);
+void topt_pattern_free(topt_pattern* p);
+
+/* ------------------------------------------------------------------------
+ * FEM handle: SIMP-scaled stiffness / conductivity, Dirichlet enforcement,
+ * preconditioned CG (FP64, or FP32-inner with FP64 iterative refinement),
+ * element energies and compliance sensitivities.
+ * Replaces FEM_SimpLinearElasticity (sktopt/fea/solver_elastic.py:540-676)
+ * and FEM_SimpLinearHeatConduction (sktopt/fea/solver_heat.py:628-980).
+ * ---------------------------------------------------------------------- */
+typedef struct topt_fem topt_fem;
+
+typedef struct topt_fem_desc {
+  int32_t bs;                 /* DOFs per node: 3 elasticity, 1 conduction   */
+  int32_t nloc;               /* nodes per element: 8 hex, 4 tet             */
+  int64_t n_nodes;
+  int64_t n_elem;
+  const int32_t* t;           /* (nloc, n_elem) row-major connectivity       */
+  const double* ke;           /* unit element matrices, n_ke x (bs*nloc)^2   */
+  int64_t n_ke;               /* 1 (shared by all elements) or n_elem        */
+  const uint8_t* dirichlet;   /* per-DOF flag (bs*n_nodes), 1 = fixed        */
+  int32_t grid[3];            /* logical cell grid for multigrid; 0 = none   */
+  const int32_t* node_ijk;    /* (3, n_nodes) logical node coords, or NULL   */
+  const int32_t* cell_of_elem;/* logical cell of each element, or NULL (id)  */
+  int32_t mixed;              /* keep an FP32 operator + hierarchy as well   */
+  int32_t mg_levels;          /* max multigrid levels (1 = no coarsening)    */
+  int32_t mg_coarse_max;      /* dense direct solve at <= this many DOFs     */
+} topt_fem_desc;
+
+int topt_fem_create(const topt_fem_desc* d, topt_fem** out);
+void topt_fem_destroy(topt_fem* h);
+int topt_fem_set_stream(topt_fem* h, void* cuda_stream);
+int topt_fem_sizes(const topt_fem* h, int64_t* n_dof, int64_t* nnzb,
+                   int32_t* n_levels);
+
+/* coef_e = Emin + (E0-Emin) rho_e^p (composer.py:19-22), K = sum coef_e Ke
+ * assembled into the fixed pattern (composer.py:53-145), Dirichlet rows and
+ * columns zeroed with unit diagonal (skfem.enforce, solver_elastic.py:211),
+ * then the preconditioner refreshed.  rho: dev, n_elem doubles. */
+int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin,
+                    double p);
+
+typedef struct topt_solve_opts {
+  int32_t method;         /* 0: FP64 PCG.  Mixed (FP32 operator, hierarchy and
+                             inner work; FP64 residual, update and dots):
+                             1: FP32 PCG with FP64 reliable updates;
+                             2: FP32 PCG restarted inside FP64 refinement;
+                             3: FP64 flexible CG around an FP32 V-cycle   */
+  int32_t precond;        /* 0: block Jacobi; 1: multigrid V-cycle           */
+  double rtol;            /* relative residual target (solver_elastic.py:37) */
+  int32_t maxiter;        /* iteration cap (per inner solve for method 2)    */
+  double inner_rtol;      /* 1: residual drop between updates; 2: inner tol  */
+  int32_t max_outer;      /* 1, 2: cap on FP64 refinement steps              */
+  int32_t cheb_degree;    /* Chebyshev smoother degree                       */
+  int32_t check_every;    /* residual check period (iterations)              */
+} topt_solve_opts;
+
+typedef struct topt_solve_info {
+  int32_t status;
+  int32_t iters;          /* FP64 PCG iterations, or inner iterations total  */
+  int32_t outer;          /* refinement steps (mixed)                        */
+  int32_t pad;
+  double relres;          /* final max over columns of ||f-Ku|| / ||f||      */
+} topt_solve_info;
+
+/* Solve K_e U = F_e for nrhs load cases (solve_u solver_elastic.py:61-143,
+ * solve_multi_load 240-395).  F, U: dev, n_dof x nrhs row-major (the layout
+ * of the reference's u_dofs); F is enforced (Dirichlet entries zeroed) in a
+ * copy; U is overwritten.  compliance (host, nrhs) receives F_e . U
+ * (solver_elastic.py:236, 465), or may be NULL. */
+int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
+                   const topt_solve_opts* o, topt_solve_info* info,
+                   double* compliance);
+
+/* y = K x with the enforced operator (dtype TOPT_F64 or TOPT_F32; F32 needs
+ * mixed).  x, y: dev, n_dof x nrhs row-major. */
+int topt_fem_spmv(topt_fem* h, int32_t dtype, const void* x, void* y,
+                  int32_t nrhs);
+
+/* Copy the enforced FP64 block values (nnzb x bs x bs) to dev memory. */
+int topt_fem_export_values(topt_fem* h, double* vals);
+
+/* Element energies 1/2 coef_e u_e^T Ke u_e (solver_elastic.py:507-537,
+ * solver_heat.py:282-303) for every load case and, when dc != NULL, the
+ * compliance sensitivity dC_drho_simp (derivatives.py:42-52) times dh
+ * (dh may be NULL = 1).  rho: the density the operator was built from.
+ * U: dev n_dof x nrhs; energy, dc: dev n_elem x nrhs row-major. */
+int topt_fem_energy(topt_fem* h, const double* U, int32_t nrhs,
+                    const double* rho, double E0, double Emin, double p,
+                    const double* dh, double* energy, double* dc);
+
+/* ------------------------------------------------------------------------
+ * Gaussian density filter (SpacialFilter, sktopt/filters/spacial.py:106-166;
+ * kernel spacial.py:37-45, matrix spacial.py:51-103).  W is built once per
+ * radius over the design elements and row-normalised.
+ * ---------------------------------------------------------------------- */
+typedef struct topt_filter topt_filter;
+int topt_filter_gauss_create(int64_t n_elem, const double* centers /* 3 x n */,
+                             const uint8_t* design_mask, double radius,
+                             topt_filter** out);
+void topt_filter_destroy(topt_filter* f);
+int topt_filter_set_stream(topt_filter* f, void* cuda_stream);
+int topt_filter_sizes(const topt_filter* f, int64_t* n_design, int64_t* nnz);
+/* host export of W (design x design CSR) for checks */
+int topt_filter_export(const topt_filter* f, int32_t* rowptr, int32_t* colind,
+                       double* vals);
+/* forward: y[design] = W x[design], y = x elsewhere (spacial.py:135-157) */
+int topt_filter_forward(topt_filter* f, const double* x, double* y);
+/* gradient: y[design] = W^T v[design], 0 elsewhere (spacial.py:159-166) */
+int topt_filter_gradient(topt_filter* f, const double* v, double* y);
+
+/* ------------------------------------------------------------------------
+ * Element-wise kernels, reductions and the density updates.
+ * ---------------------------------------------------------------------- */
+/* Heaviside projection and derivative (projection.py:27-118); either output
+ * may be NULL. */
+int topt_projection(int64_t n, const double* x, double beta, double eta,
+                    double* h, double* dh, void* stream);
+
+/* OC bisection on the volume multiplier (oc.py:16-95) with the filter and
+ * projection applied to every candidate.  The design set is the filter's.
+ * dc: full-length sensitivities, divided by dc_scale on the fly (the
+ * running-scale normalisation of oc.py:186-196); rho: full-length density,
+ * its design entries replaced by the accepted candidate; vol: design-element
+ * volumes (design order).  scaling (design order, may be NULL) receives the
+ * clipped multiplicative factor; lmid, vol_error, steps (host) the
+ * bisection result. */
+typedef struct topt_oc_params {
+  double rho_min, rho_max, move_limit, eta, eps, vol_frac, beta, beta_eta;
+  double scaling_min, scaling_max, vol_tol, l1, l2, tolerance;
+  int32_t max_iter;
+  int32_t pad;
+} topt_oc_params;
+int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rho,
+                   const double* vol, double vol_sum, const topt_oc_params* prm,
+                   double* scaling, double* lmid, double* vol_error, int32_t* steps);
+
+/* Reductions over the filter's design elements (host result):
+ * op 0: max |x[d]|            (oc.py:186-191 sensitivity scale)
+ * op 1: max |x[d] - y[d]|     (common_density.py:1137-1141 rho_change_max)
+ * op 2: max |x[d] + c w[i]| over interior y[d] in (rho_min+1e-6, rho_max-1e-6)
+ *       (oc.py:230-240 KKT residual; w in design order). */
+int topt_design_reduce(topt_filter* f, int32_t op, const double* x, const double* y,
+                       const double* w, double c, double rho_min, double rho_max,
+                       double* out);
+
+/* Deterministic reductions (host result). */
+int topt_reduce_max_abs(int64_t n, const double* x, double* out, void* stream);
+int topt_reduce_dot(int64_t n, const double* x, const double* y, double* out,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

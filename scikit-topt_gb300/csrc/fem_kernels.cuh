@@ -1,0 +1,842 @@
+// Device kernels of the FEM engine: SIMP coefficients, fixed-pattern BSR
+// assembly with Dirichlet enforcement, BSR SpMV/SpMM, PCG vector updates,
+// block-Jacobi, Chebyshev smoothing, structured-grid transfer operators,
+// element-level Galerkin coarsening, dense coarsest solve and element
+// energies.  Vectors with several load cases are stored n_dof x L row-major
+// (value of DOF i, load j at i*L + j), the layout of the reference's u_dofs.
+#pragma once
+
+#include "cuda_common.cuh"
+
+namespace topt {
+
+// --------------------------------------------------------------------------
+// SIMP coefficient E(rho) = Emin + (E0 - Emin) rho^p  (composer.py:19-22)
+__global__ void k_simp_coef(int64_t n, const double* __restrict__ rho, double E0,
+                            double Emin, double p, double* __restrict__ c64,
+                            float* __restrict__ c32) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double r = rho[i];
+    const double v = Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
+    if (c64) c64[i] = v;
+    if (c32) c32[i] = (float)v;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Sliced-ELL block storage (SELL-32, bs x bs blocks).  Block rows (nodes) are
+// grouped in slices of 32; every slice is padded to its longest row and
+// stored column by column, so block j of the 32 rows of a slice occupies one
+// "group" of 32 consecutive positions.  Block values are stored plane by
+// plane inside a group: value v of the block at position p lives at
+// ((p >> 5) * bs*bs + v) * 32 + (p & 31), so a warp reads each plane with
+// one coalesced 32-wide access.  Padding blocks point at their own row and
+// hold zeros.
+struct SellT {
+  int64_t nrows;
+  const int32_t* grp_of_slice;  // nslices + 1
+  const int32_t* slice_of_grp;  // ngroups
+  const int32_t* col;           // npos
+  const int32_t* rowlen;        // nrows
+  const int32_t* diag;          // nrows, position of the diagonal block
+};
+
+template <int BS>
+__device__ __forceinline__ int64_t vidx(int64_t p, int v) {
+  return ((p >> 5) * (BS * BS) + v) * 32 + (p & 31);
+}
+
+// Fixed-pattern assembly: one thread per block position sums its element
+// contributions in ascending element order (deterministic, no atomics).
+// ke_stride == 0 means one matrix shared by all elements (kept in shared
+// memory).  mask (per DOF) applies skfem.enforce: rows and columns of fixed
+// DOFs are zeroed and their diagonal set to 1.
+template <typename T, int BS, int NLOC>
+__global__ void k_assemble(int64_t npos, SellT sp, const int64_t* __restrict__ cptr,
+                           const int32_t* __restrict__ contrib,
+                           const T* __restrict__ ke, int64_t ke_stride,
+                           const T* __restrict__ coef, const uint8_t* __restrict__ mask,
+                           T* __restrict__ vals) {
+  TOPT_KERNEL_COUNT();
+  constexpr int ND = BS * NLOC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* kes = reinterpret_cast<T*>(smem_raw);
+  if (ke_stride == 0) {
+    for (int i = threadIdx.x; i < ND * ND; i += blockDim.x) kes[i] = ke[i];
+    __syncthreads();
+  }
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npos;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    T acc[BS * BS];
+#pragma unroll
+    for (int i = 0; i < BS * BS; ++i) acc[i] = T(0);
+    const int64_t c1 = cptr[k + 1];
+    for (int64_t c = cptr[k]; c < c1; ++c) {
+      const int32_t code = contrib[c];
+      const int32_t e = code / (NLOC * NLOC);
+      const int r = code - e * (NLOC * NLOC);
+      const int la = r / NLOC, lb = r - la * NLOC;
+      const T* K = ke_stride ? ke + (int64_t)e * ke_stride : kes;
+      const T s = coef ? coef[e] : T(1);
+#pragma unroll
+      for (int c0 = 0; c0 < BS; ++c0)
+#pragma unroll
+        for (int d0 = 0; d0 < BS; ++d0)
+          acc[c0 * BS + d0] += s * K[(BS * la + c0) * ND + BS * lb + d0];
+    }
+    if (mask) {
+      const int64_t a = (int64_t)sp.slice_of_grp[k >> 5] * 32 + (k & 31);
+      if (a < sp.nrows) {
+        const int64_t b = sp.col[k];
+        const bool is_diag = (sp.diag[a] == k);
+#pragma unroll
+        for (int c0 = 0; c0 < BS; ++c0)
+#pragma unroll
+          for (int d0 = 0; d0 < BS; ++d0) {
+            const bool ma = mask[BS * a + c0], mb = mask[BS * b + d0];
+            if (ma || mb) acc[c0 * BS + d0] = (is_diag && c0 == d0 && ma) ? T(1) : T(0);
+          }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < BS * BS; ++i) vals[vidx<BS>(k, i)] = acc[i];
+  }
+}
+
+// Coarse levels: a DOF whose prolongation column is empty has an all-zero
+// row and column; give it a unit diagonal so the level stays nonsingular.
+template <typename T, int BS>
+__global__ void k_fix_zero_diag(SellT sp, T* __restrict__ vals) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < sp.nrows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pd = sp.diag[i];
+#pragma unroll
+    for (int c = 0; c < BS; ++c)
+      if (vals[vidx<BS>(pd, c * BS + c)] == T(0)) vals[vidx<BS>(pd, c * BS + c)] = T(1);
+  }
+}
+
+// Inverse of every diagonal block (block Jacobi), computed in double.
+template <typename T, int BS>
+__global__ void k_block_diag_inv(SellT sp, const T* __restrict__ vals, T* __restrict__ dinv) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < sp.nrows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t pd = sp.diag[i];
+    T* O = dinv + i * BS * BS;
+    if (BS == 1) {
+      const double d = (double)vals[vidx<BS>(pd, 0)];
+      O[0] = (T)(d != 0.0 ? 1.0 / d : 0.0);
+    } else {
+      double D[9];
+#pragma unroll
+      for (int v = 0; v < 9; ++v) D[v] = (double)vals[vidx<BS>(pd, v)];
+      const double a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5],
+                   g = D[6], h = D[7], k = D[8];
+      const double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+      const double det = a * A + b * B + c * C;
+      const double s = det != 0.0 ? 1.0 / det : 0.0;
+      O[0] = (T)(A * s);
+      O[1] = (T)(-(b * k - c * h) * s);
+      O[2] = (T)((b * f - c * e) * s);
+      O[3] = (T)(B * s);
+      O[4] = (T)((a * k - c * g) * s);
+      O[5] = (T)(-(a * f - c * d) * s);
+      O[6] = (T)(C * s);
+      O[7] = (T)(-(a * h - b * g) * s);
+      O[8] = (T)((a * e - b * d) * s);
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// SELL-32 BSR SpMV / SpMM: one thread per block row, no cross-lane
+// reduction; every plane load of a warp is one coalesced 32-wide access.
+// MODE 0: y = A x;  MODE 1: y = b - A x;  MODE 2: y = y - A x.
+// DOT: also reduce sum_j (x_row . y_row) per load into dot_out (fused p.Ap).
+template <typename T, int BS, int L, int MODE, bool DOT>
+__global__ void __launch_bounds__(256)
+k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
+            const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
+            double* dot_out) {
+  TOPT_KERNEL_COUNT();
+  double dacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+       row < ((sp.nrows + 31) & ~(int64_t)31); row += nthreads) {
+    const int64_t slice = row >> 5;
+    const int lane = (int)(row & 31);
+    const int64_t g0 = sp.grp_of_slice[slice], g1 = sp.grp_of_slice[slice + 1];
+    T acc[BS * L];
+#pragma unroll
+    for (int i = 0; i < BS * L; ++i) acc[i] = T(0);
+#pragma unroll 3
+    for (int64_t g = g0; g < g1; ++g) {
+      const int64_t col = sp.col[g * 32 + lane];
+      const T* V = vals + g * (BS * BS * 32) + lane;
+      T xv[BS * L];
+#pragma unroll
+      for (int i = 0; i < BS * L; ++i) xv[i] = x[col * BS * L + i];
+#pragma unroll
+      for (int c = 0; c < BS; ++c)
+#pragma unroll
+        for (int d = 0; d < BS; ++d) {
+          const T a = V[(c * BS + d) * 32];
+#pragma unroll
+          for (int j = 0; j < L; ++j) acc[c * L + j] += a * xv[d * L + j];
+        }
+    }
+    if (row < sp.nrows) {
+#pragma unroll
+      for (int i = 0; i < BS * L; ++i) {
+        const int64_t idx = row * BS * L + i;
+        T out;
+        if (MODE == 0) out = acc[i];
+        else if (MODE == 1) out = b[idx] - acc[i];
+        else out = y[idx] - acc[i];
+        y[idx] = out;
+        if (DOT) dacc[i % L] += (double)x[idx] * (double)out;
+      }
+    }
+  }
+  if (DOT) {
+    __shared__ double sh[32 * L];
+    block_sum<double, L>(dacc, sh);
+    grid_finish<double, L>(dacc, partials, counter, dot_out);
+  }
+}
+
+// CSR-order copy of the SELL values (the CSR stays the interface object).
+template <int BS>
+__global__ void k_sell_to_csr(int64_t nnzb, const int32_t* __restrict__ csr2sell,
+                              const double* __restrict__ vals, double* __restrict__ out) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnzb;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = csr2sell[k];
+#pragma unroll
+    for (int v = 0; v < BS * BS; ++v) out[k * BS * BS + v] = vals[vidx<BS>(p, v)];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Vector kernels (n = number of DOFs; vectors n x L).
+
+// z = Dinv r  and, optionally, partial sums of r.z per load.
+template <typename T, int BS, int L, bool DOT>
+__global__ void k_block_jacobi(int64_t n_nodes, const T* __restrict__ dinv,
+                               const T* __restrict__ r, T* __restrict__ z,
+                               double* partials, unsigned* counter, double* dot_out) {
+  TOPT_KERNEL_COUNT();
+  double dacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T* D = dinv + i * BS * BS;
+    T rv[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) rv[q] = r[i * BS * L + q];
+#pragma unroll
+    for (int c = 0; c < BS; ++c)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        T s = T(0);
+#pragma unroll
+        for (int d = 0; d < BS; ++d) s += D[c * BS + d] * rv[d * L + j];
+        z[i * BS * L + c * L + j] = s;
+        if (DOT) dacc[j] += (double)s * (double)rv[c * L + j];
+      }
+  }
+  if (DOT) {
+    __shared__ double sh[32 * L];
+    block_sum<double, L>(dacc, sh);
+    grid_finish<double, L>(dacc, partials, counter, dot_out);
+  }
+}
+
+// Deterministic dot products per load: out[j] = sum_i x[i,j] y[i,j].
+template <typename T, int L>
+__global__ void k_dot(int64_t n, const T* __restrict__ x, const T* __restrict__ y,
+                      double* partials, unsigned* counter, double* out) {
+  TOPT_KERNEL_COUNT();
+  double acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) acc[j] += (double)x[i * L + j] * (double)y[i * L + j];
+  }
+  __shared__ double sh[32 * L];
+  block_sum<double, L>(acc, sh);
+  grid_finish<double, L>(acc, partials, counter, out);
+}
+
+// PCG update: alpha_j = rz_j / pq_j (0 when frozen or pq <= 0);
+// x += alpha p; r -= alpha q; partial sums of r.r.
+template <typename T, int L>
+__global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
+                             const double* __restrict__ pq, const int* __restrict__ active,
+                             const T* __restrict__ p, const T* __restrict__ q,
+                             T* __restrict__ x, T* __restrict__ r, double* partials,
+                             unsigned* counter, double* rr_out) {
+  TOPT_KERNEL_COUNT();
+  T alpha[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) {
+    const double d = pq[j];
+    alpha[j] = (active[j] && d > 0.0) ? (T)(rz[j] / d) : T(0);
+  }
+  double acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      const int64_t q_ = i * L + j;
+      x[q_] += alpha[j] * p[q_];
+      const T rv = r[q_] - alpha[j] * q[q_];
+      r[q_] = rv;
+      acc[j] += (double)rv * (double)rv;
+    }
+  }
+  __shared__ double sh[32 * L];
+  block_sum<double, L>(acc, sh);
+  grid_finish<double, L>(acc, partials, counter, rr_out);
+}
+
+// Two dots sharing z: out[0..L) = r.z, out[L..2L) = q.z (flexible CG).
+template <typename T, int L>
+__global__ void k_dot2(int64_t n, const T* __restrict__ r, const T* __restrict__ q,
+                       const T* __restrict__ z, double* partials, unsigned* counter,
+                       double* out) {
+  TOPT_KERNEL_COUNT();
+  double acc[2 * L];
+#pragma unroll
+  for (int j = 0; j < 2 * L; ++j) acc[j] = 0.0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      const double zv = (double)z[i * L + j];
+      acc[j] += (double)r[i * L + j] * zv;
+      acc[L + j] += (double)q[i * L + j] * zv;
+    }
+  }
+  __shared__ double sh[32 * 2 * L];
+  block_sum<double, 2 * L>(acc, sh);
+  grid_finish<double, 2 * L>(acc, partials, counter, out);
+}
+
+// Flexible (Polak-Ribiere) direction: beta_j = -alpha_j (q.z_new)_j / rz_old_j
+// with alpha_j = rz_old_j / pq_j, i.e. beta = -(q.z_new) / pq; p = z + beta p.
+template <typename T, int L>
+__global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
+                                const double* __restrict__ pq, const int* __restrict__ active,
+                                const T* __restrict__ z, T* __restrict__ p) {
+  TOPT_KERNEL_COUNT();
+  T beta[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j)
+    beta[j] = (active[j] && pq[j] > 0.0) ? (T)(-qz[j] / pq[j]) : T(0);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) p[i * L + j] = z[i * L + j] + beta[j] * p[i * L + j];
+  }
+}
+
+// p = z + beta p with beta_j = rz_new_j / rz_old_j (p = z on the first step).
+template <typename T, int L>
+__global__ void k_pcg_direction(int64_t n, const double* __restrict__ rz_new,
+                                const double* __restrict__ rz_old, int first,
+                                const T* __restrict__ z, T* __restrict__ p) {
+  TOPT_KERNEL_COUNT();
+  T beta[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j)
+    beta[j] = (first || rz_old[j] == 0.0) ? T(0) : (T)(rz_new[j] / rz_old[j]);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j)   // p = z exactly on the first step (p may hold garbage)
+      p[i * L + j] = first ? z[i * L + j] : z[i * L + j] + beta[j] * p[i * L + j];
+  }
+}
+
+// Chebyshev smoothing steps (Saad, Iterative Methods, Alg. 12.1):
+// first: d = c2 Dinv r; x = d (x_zero) or x += d.
+// next:  d = c1 d + c2 Dinv r; x += d.
+template <typename T, int BS, int L>
+__global__ void k_cheb(int64_t n_nodes, const T* __restrict__ dinv,
+                       const T* __restrict__ r, T* __restrict__ d, T* __restrict__ x,
+                       T c1, T c2, int first, int x_zero) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const T* D = dinv + i * BS * BS;
+    T rv[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) rv[q] = r[i * BS * L + q];
+#pragma unroll
+    for (int c = 0; c < BS; ++c)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        T s = T(0);
+#pragma unroll
+        for (int dd = 0; dd < BS; ++dd) s += D[c * BS + dd] * rv[dd * L + j];
+        const int64_t q_ = i * BS * L + c * L + j;
+        const T dv = first ? c2 * s : c1 * d[q_] + c2 * s;
+        d[q_] = dv;
+        x[q_] = (first && x_zero) ? dv : x[q_] + dv;
+      }
+  }
+}
+
+// Elementwise helpers.
+template <typename TO, typename TI>
+__global__ void k_convert(int64_t n, const TI* __restrict__ a, TO* __restrict__ b) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (TO)a[i];
+}
+template <typename T>
+__global__ void k_fill(int64_t n, T v, T* __restrict__ a) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = v;
+}
+// U += double(d)
+__global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
+                                 double* __restrict__ u) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    u[i] += (double)d[i];
+}
+// F_e: copy of F with fixed DOFs zeroed (enforce's RHS with x = 0).
+__global__ void k_enforce_rhs(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
+                              const double* __restrict__ f, double* __restrict__ fe) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof * L;
+       i += (int64_t)gridDim.x * blockDim.x)
+    fe[i] = mask[i / L] ? 0.0 : f[i];
+}
+// Deterministic pseudo-random start vector for the power iteration.
+template <typename T>
+__global__ void k_hash_fill(int64_t n, T* __restrict__ a) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    uint64_t h = (uint64_t)i * 0x9E3779B97F4A7C15ull + 0x2545F4914F6CDD1Dull;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    a[i] = (T)(0.5 + (double)(h >> 11) * (1.0 / 9007199254740992.0));
+  }
+}
+
+// --------------------------------------------------------------------------
+// Structured-grid transfers.  Level grids number nodes iy + (ny+1)(ix +
+// (nx+1) iz).  Per axis, cm[i] is the fine node index of coarse node i,
+// c0[f] the coarse interval holding fine node f and w1[f] the weight of its
+// right end.  mask (fine DOFs, level 0 only) removes fixed DOFs from P.
+struct GridT {
+  int nfx, nfy, nfz;  // fine cells
+  int ncx, ncy, ncz;  // coarse cells
+  const int32_t *cmx, *cmy, *cmz;
+  const int32_t *c0x, *c0y, *c0z;
+  const double *w1x, *w1y, *w1z;
+};
+
+__device__ __forceinline__ double restrict_w(int f, int i, const int32_t* cm, int nc) {
+  const int ci = cm[i];
+  if (f == ci) return 1.0;
+  if (f < ci) {
+    if (i == 0) return 0.0;
+    const int cl = cm[i - 1];
+    return f > cl ? (double)(f - cl) / (double)(ci - cl) : 0.0;
+  }
+  if (i == nc) return 0.0;
+  const int cr = cm[i + 1];
+  return f < cr ? (double)(cr - f) / (double)(cr - ci) : 0.0;
+}
+
+// bc = P^T r  (coarse node gathers its fine support, fixed order)
+template <typename T, int BS, int L>
+__global__ void k_restrict(GridT g, const uint8_t* __restrict__ mask,
+                           const T* __restrict__ rf, T* __restrict__ bc) {
+  TOPT_KERNEL_COUNT();
+  const int64_t nnx = g.ncx + 1, nny = g.ncy + 1, nnz_ = g.ncz + 1;
+  const int64_t nc = nnx * nny * nnz_;
+  const int64_t fnx = g.nfx + 1, fny = g.nfy + 1;
+  for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc;
+       I += (int64_t)gridDim.x * blockDim.x) {
+    const int iy = (int)(I % nny);
+    const int ix = (int)((I / nny) % nnx);
+    const int iz = (int)(I / (nny * nnx));
+    const int fx0 = ix > 0 ? g.cmx[ix - 1] + 1 : 0, fx1 = ix < g.ncx ? g.cmx[ix + 1] - 1 : g.nfx;
+    const int fy0 = iy > 0 ? g.cmy[iy - 1] + 1 : 0, fy1 = iy < g.ncy ? g.cmy[iy + 1] - 1 : g.nfy;
+    const int fz0 = iz > 0 ? g.cmz[iz - 1] + 1 : 0, fz1 = iz < g.ncz ? g.cmz[iz + 1] - 1 : g.nfz;
+    T acc[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) acc[q] = T(0);
+    for (int fz = fz0; fz <= fz1; ++fz) {
+      const double wz = restrict_w(fz, iz, g.cmz, g.ncz);
+      for (int fx = fx0; fx <= fx1; ++fx) {
+        const double wx = restrict_w(fx, ix, g.cmx, g.ncx) * wz;
+        for (int fy = fy0; fy <= fy1; ++fy) {
+          const T w = (T)(restrict_w(fy, iy, g.cmy, g.ncy) * wx);
+          const int64_t fn = fy + fny * (fx + fnx * (int64_t)fz);
+#pragma unroll
+          for (int c = 0; c < BS; ++c) {
+            if (mask && mask[fn * BS + c]) continue;
+#pragma unroll
+            for (int j = 0; j < L; ++j) acc[c * L + j] += w * rf[(fn * BS + c) * L + j];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) bc[I * BS * L + q] = acc[q];
+  }
+}
+
+// xf += P xc
+template <typename T, int BS, int L>
+__global__ void k_prolong_add(GridT g, const uint8_t* __restrict__ mask,
+                              const T* __restrict__ xc, T* __restrict__ xf) {
+  TOPT_KERNEL_COUNT();
+  const int64_t fnx = g.nfx + 1, fny = g.nfy + 1, fnz = g.nfz + 1;
+  const int64_t nf = fnx * fny * fnz;
+  const int64_t cnx = g.ncx + 1, cny = g.ncy + 1;
+  for (int64_t F = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; F < nf;
+       F += (int64_t)gridDim.x * blockDim.x) {
+    const int fy = (int)(F % fny);
+    const int fx = (int)((F / fny) % fnx);
+    const int fz = (int)(F / (fny * fnx));
+    const int cx = g.c0x[fx], cy = g.c0y[fy], cz = g.c0z[fz];
+    const double ax = g.w1x[fx], ay = g.w1y[fy], az = g.w1z[fz];
+    T acc[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) acc[q] = T(0);
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz) {
+      const double wz = oz ? az : 1.0 - az;
+      if (wz == 0.0) continue;
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const double wx = (ox ? ax : 1.0 - ax) * wz;
+        if (wx == 0.0) continue;
+#pragma unroll
+        for (int oy = 0; oy < 2; ++oy) {
+          const double wd = (oy ? ay : 1.0 - ay) * wx;
+          if (wd == 0.0) continue;
+          const T w = (T)wd;
+          const int64_t cn = (cy + oy) + cny * ((cx + ox) + cnx * (int64_t)(cz + oz));
+#pragma unroll
+          for (int q = 0; q < BS * L; ++q) acc[q] += w * xc[cn * BS * L + q];
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < BS; ++c) {
+      if (mask && mask[F * BS + c]) continue;
+#pragma unroll
+      for (int j = 0; j < L; ++j) xf[(F * BS + c) * L + j] += acc[c * L + j];
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Element-level Galerkin coarsening: for every coarse cell C,
+//   Kc = sum_{fine elements e in C} coef_e P_e^T Ke P_e,
+// with P_e the masked trilinear interpolation from C's 8 corners (MeshHex
+// local order) to e's nodes.  One CTA per coarse cell; fine elements are the
+// hex cells of the finer grid (cell_ptr == nullptr) or the elements listed
+// per fine cell.
+__constant__ int c_hex_off[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1},
+                                    {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 1}};
+
+template <typename T, int BS, int NLOC>
+__global__ void __launch_bounds__(256)
+k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
+           const int32_t* __restrict__ cell_ptr,
+           const int32_t* __restrict__ cell_elems, const int32_t* __restrict__ t,
+           int64_t n_elem_f, const T* __restrict__ ke, int64_t ke_stride,
+           const T* __restrict__ coef, const uint8_t* __restrict__ mask,
+           T* __restrict__ kc) {
+  TOPT_KERNEL_COUNT();
+  constexpr int NF = BS * NLOC;   // fine element DOFs
+  constexpr int NC = BS * 8;      // coarse cell DOFs
+  __shared__ T Ks[NF * NF];
+  __shared__ T Wm[NLOC * 8];
+  __shared__ T Mk[NF];
+  __shared__ T Tm[NF * NC];
+  __shared__ T sc;
+  const int64_t C = cell_list ? (int64_t)cell_list[blockIdx.x] : (int64_t)blockIdx.x;
+  const int Cy = (int)(C % g.ncy);
+  const int Cx = (int)((C / g.ncy) % g.ncx);
+  const int Cz = (int)(C / ((int64_t)g.ncy * g.ncx));
+  const int ax0 = g.cmx[Cx], ax1 = g.cmx[Cx + 1];
+  const int ay0 = g.cmy[Cy], ay1 = g.cmy[Cy + 1];
+  const int az0 = g.cmz[Cz], az1 = g.cmz[Cz + 1];
+  const int64_t fny = g.nfy + 1, fnx = g.nfx + 1;
+  constexpr int PER = (NC * NC + 255) / 256;
+  T acc[PER];
+#pragma unroll
+  for (int q = 0; q < PER; ++q) acc[q] = T(0);
+  if (ke_stride == 0) {
+    for (int i = threadIdx.x; i < NF * NF; i += blockDim.x) Ks[i] = ke[i];
+  }
+  for (int fz = az0; fz < az1; ++fz)
+    for (int fx = ax0; fx < ax1; ++fx)
+      for (int fy = ay0; fy < ay1; ++fy) {
+        const int64_t fc = fy + (int64_t)g.nfy * (fx + (int64_t)g.nfx * fz);
+        const int64_t e0 = cell_ptr ? cell_ptr[fc] : fc;
+        const int64_t e1 = cell_ptr ? cell_ptr[fc + 1] : fc + 1;
+        for (int64_t ei = e0; ei < e1; ++ei) {
+          const int64_t e = cell_ptr ? cell_elems[ei] : ei;
+          __syncthreads();
+          if (ke_stride != 0)
+            for (int i = threadIdx.x; i < NF * NF; i += blockDim.x)
+              Ks[i] = ke[e * ke_stride + i];
+          if (threadIdx.x < NLOC * 8) {
+            const int a = threadIdx.x / 8, k = threadIdx.x % 8;
+            const int64_t n = t[(int64_t)a * n_elem_f + e];
+            const int iy = (int)(n % fny), ix = (int)((n / fny) % fnx),
+                      iz = (int)(n / (fny * fnx));
+            const double xi = (double)(ix - ax0) / (double)(ax1 - ax0);
+            const double yi = (double)(iy - ay0) / (double)(ay1 - ay0);
+            const double zi = (double)(iz - az0) / (double)(az1 - az0);
+            const double w = (c_hex_off[k][0] ? xi : 1.0 - xi) *
+                             (c_hex_off[k][1] ? yi : 1.0 - yi) *
+                             (c_hex_off[k][2] ? zi : 1.0 - zi);
+            Wm[a * 8 + k] = (T)w;
+          }
+          if (threadIdx.x < NF) {
+            const int a = threadIdx.x / BS, c = threadIdx.x % BS;
+            const int64_t n = t[(int64_t)a * n_elem_f + e];
+            Mk[threadIdx.x] = (mask && mask[n * BS + c]) ? T(0) : T(1);
+          }
+          if (threadIdx.x == 0) sc = coef ? coef[e] : T(1);
+          __syncthreads();
+          // Tm[(a,c),(l,d)] = sum_b Ks[(a,c),(b,d)] Mk[(b,d)] W[b][l]
+          for (int i = threadIdx.x; i < NF * NC; i += blockDim.x) {
+            const int row = i / NC, col = i % NC;
+            const int l = col / BS, d = col % BS;
+            T s = T(0);
+#pragma unroll
+            for (int b = 0; b < NLOC; ++b)
+              s += Ks[row * NF + b * BS + d] * Mk[b * BS + d] * Wm[b * 8 + l];
+            Tm[i] = s;
+          }
+          __syncthreads();
+          const T scale = sc;
+#pragma unroll
+          for (int q = 0; q < PER; ++q) {
+            const int i = threadIdx.x + q * 256;
+            if (i < NC * NC) {
+              const int row = i / NC, col = i % NC;
+              const int k = row / BS, c = row % BS;
+              T s = T(0);
+#pragma unroll
+              for (int a = 0; a < NLOC; ++a)
+                s += Wm[a * 8 + k] * Mk[a * BS + c] * Tm[(a * BS + c) * NC + col];
+              acc[q] += scale * s;
+            }
+          }
+        }
+      }
+#pragma unroll
+  for (int q = 0; q < PER; ++q) {
+    const int i = threadIdx.x + q * 256;
+    if (i < NC * NC) kc[C * NC * NC + i] = acc[q];
+  }
+}
+
+// Galerkin coarsening when every fine element is a hex cell sharing one unit
+// matrix K0: P_c^T (coef K0) P_c = coef M[pattern][child] with M precomputed
+// for the 8 coarse-cell extent patterns (1 or 2 fine cells per axis) and the
+// 8 child positions, so Kc = sum_children coef_child M.  Cells touching fixed
+// DOFs (masked interpolation) are skipped here and done by k_galerkin.
+template <typename T, int BS>
+__global__ void __launch_bounds__(192)
+k_galerkin_shared(GridT g, const uint8_t* __restrict__ cell_masked, const T* __restrict__ M,
+                  const T* __restrict__ coef, T* __restrict__ kc) {
+  TOPT_KERNEL_COUNT();
+  constexpr int NC = BS * 8;
+  constexpr int NN = NC * NC;
+  const int64_t ncells = (int64_t)g.ncx * g.ncy * g.ncz;
+  for (int64_t C = blockIdx.x; C < ncells; C += gridDim.x) {
+    if (cell_masked[C]) continue;
+    const int Cy = (int)(C % g.ncy);
+    const int Cx = (int)((C / g.ncy) % g.ncx);
+    const int Cz = (int)(C / ((int64_t)g.ncy * g.ncx));
+    const int x0 = g.cmx[Cx], ex = g.cmx[Cx + 1] - x0;
+    const int y0 = g.cmy[Cy], ey = g.cmy[Cy + 1] - y0;
+    const int z0 = g.cmz[Cz], ez = g.cmz[Cz + 1] - z0;
+    const int pat = (ex - 1) + 2 * (ey - 1) + 4 * (ez - 1);
+    T cf[8];
+    int nchild = 0;
+#pragma unroll
+    for (int ch = 0; ch < 8; ++ch) {
+      const int ox = ch & 1, oy = (ch >> 1) & 1, oz = ch >> 2;
+      const bool ok = ox < ex && oy < ey && oz < ez;
+      const int64_t fc = (y0 + oy) + (int64_t)g.nfy * ((x0 + ox) + (int64_t)g.nfx * (z0 + oz));
+      cf[ch] = ok ? coef[fc] : T(0);
+      nchild += ok;
+    }
+    (void)nchild;
+    const T* Mp = M + (int64_t)pat * 8 * NN;
+    for (int i = threadIdx.x; i < NN; i += blockDim.x) {
+      T acc = T(0);
+#pragma unroll
+      for (int ch = 0; ch < 8; ++ch) acc += cf[ch] * Mp[ch * NN + i];
+      kc[C * NN + i] = acc;
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Dense coarsest level: BSR -> dense, in-place Gauss-Jordan inverse (one CTA,
+// SPD so no pivoting), dense mat-vec.
+template <typename T, int BS>
+__global__ void k_sell_to_dense(int64_t npos, SellT sp, const T* __restrict__ vals, int n,
+                                double* __restrict__ A) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < npos;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t slice = sp.slice_of_grp[k >> 5];
+    const int64_t a = slice * 32 + (k & 31);
+    if (a >= sp.nrows) continue;
+    const int64_t j = (k >> 5) - sp.grp_of_slice[slice];
+    if (j >= sp.rowlen[a]) continue;
+    const int64_t b = sp.col[k];
+#pragma unroll
+    for (int c = 0; c < BS; ++c)
+#pragma unroll
+      for (int d = 0; d < BS; ++d)
+        A[(a * BS + c) * n + b * BS + d] = (double)vals[vidx<BS>(k, c * BS + d)];
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_gauss_jordan_inverse(int n, double* __restrict__ A) {
+  TOPT_KERNEL_COUNT();
+  __shared__ double pivinv;
+  for (int k = 0; k < n; ++k) {
+    if (threadIdx.x == 0) {
+      const double pv = A[(int64_t)k * n + k];
+      pivinv = pv != 0.0 ? 1.0 / pv : 0.0;
+      A[(int64_t)k * n + k] = 1.0;
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += blockDim.x) A[(int64_t)k * n + j] *= pivinv;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < n * n; idx += blockDim.x) {
+      const int i = idx / n, j = idx % n;
+      if (i == k || j == k) continue;
+      A[(int64_t)i * n + j] -= A[(int64_t)i * n + k] * A[(int64_t)k * n + j];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+      if (i != k) A[(int64_t)i * n + k] = -A[(int64_t)i * n + k] * A[(int64_t)k * n + k];
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void k_dense_copy(int64_t nn, const double* __restrict__ A, T* __restrict__ B) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nn;
+       i += (int64_t)gridDim.x * blockDim.x)
+    B[i] = (T)A[i];
+}
+
+// x = Ainv b for L loads; one warp per output row.
+template <typename T, int L>
+__global__ void k_dense_matvec(int n, const T* __restrict__ Ainv, const T* __restrict__ b,
+                               T* __restrict__ x) {
+  TOPT_KERNEL_COUNT();
+  const int lane = threadIdx.x & 31;
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (w >= n) return;
+  T acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = T(0);
+  for (int c = lane; c < n; c += 32) {
+    const T a = Ainv[(int64_t)w * n + c];
+#pragma unroll
+    for (int j = 0; j < L; ++j) acc[j] += a * b[(int64_t)c * L + j];
+  }
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = warp_sum(acc[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) x[(int64_t)w * L + j] = acc[j];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Element energies and compliance sensitivities (one thread per element):
+// q = u_e^T Ke u_e, energy = 1/2 coef q (solver_elastic.py:470-537),
+// dc = dC_drho_simp(rho, energy) (derivatives.py:25-52) times dh.
+template <int BS, int NLOC>
+__global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
+                         const double* __restrict__ ke, int64_t ke_stride,
+                         const double* __restrict__ U, const double* __restrict__ rho,
+                         double E0, double Emin, double p, const double* __restrict__ dh,
+                         double* __restrict__ energy, double* __restrict__ dc) {
+  TOPT_KERNEL_COUNT();
+  constexpr int ND = BS * NLOC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* kes = reinterpret_cast<double*>(smem_raw);
+  if (ke_stride == 0) {
+    for (int i = threadIdx.x; i < ND * ND; i += blockDim.x) kes[i] = ke[i];
+    __syncthreads();
+  }
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const double* K = ke_stride ? ke + e * ke_stride : kes;
+    int64_t node[NLOC];
+#pragma unroll
+    for (int a = 0; a < NLOC; ++a) node[a] = t[(int64_t)a * ne + e];
+    const double r = rho[e];
+    const double coef = Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
+    const double rc = fmax(r, 1e-6);
+    const double rp1 = (p == 3.0) ? rc * rc : pow(rc, p - 1.0);
+    const double dE = p * (E0 - Emin) * rp1;
+    const double Ec = fmax(Emin + (E0 - Emin) * rp1 * rc, 1e-12);
+    const double h = dh ? dh[e] : 1.0;
+    for (int j = 0; j < L; ++j) {
+      double u[ND];
+#pragma unroll
+      for (int a = 0; a < NLOC; ++a)
+#pragma unroll
+        for (int c = 0; c < BS; ++c) u[a * BS + c] = U[(node[a] * BS + c) * L + j];
+      double q = 0.0;
+#pragma unroll
+      for (int i = 0; i < ND; ++i) {
+        double s = 0.5 * K[i * ND + i] * u[i];
+#pragma unroll
+        for (int k = i + 1; k < ND; ++k) s += K[i * ND + k] * u[k];
+        q += u[i] * s;
+      }
+      q *= 2.0;
+      const double en = 0.5 * coef * q;
+      if (energy) energy[e * L + j] = en;
+      if (dc) dc[e * L + j] = (-2.0 * en * dE / Ec) * h;
+    }
+  }
+}
+
+}  // namespace topt

@@ -1,0 +1,649 @@
+// Gaussian density filter, Heaviside projection, OC bisection, LogMOC update
+// and deterministic reductions.
+//
+// Replaces SpacialFilter (sktopt/filters/spacial.py:19-166), the projection
+// functions (sktopt/core/projection.py:27-118), bisection_with_physical_volume
+// (sktopt/core/optimizers/oc.py:16-95) and lagrangian_log_update
+// (sktopt/core/optimizers/logmoc.py:36-66).
+#include "cuda_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <memory>
+#include <new>
+#include <unordered_map>
+#include <vector>
+
+namespace topt {
+
+static const int kFB = 256;
+
+struct OcState {
+  double l1, l2, lmid, vol_error;
+  int it, done, steps, pad;
+};
+
+}  // namespace topt
+
+struct topt_filter {
+  int64_t n_elem = 0, n_design = 0, nnz = 0;
+  cudaStream_t stream = nullptr;
+  int sm = 152;
+  std::vector<int32_t> h_rowptr, h_colind;   // design-local columns
+  std::vector<double> h_vals;
+  topt::DevBuf design, nondesign;            // element ids
+  topt::DevBuf rowptr, colfull, vals;        // W with full-element columns
+  topt::DevBuf t_rowptr, t_colfull, t_vals;  // W^T
+  int64_t n_nondesign = 0;
+  // OC work
+  topt::DevBuf cand, state, partials, counter, rho_e, rho_new;
+};
+
+namespace topt {
+
+// --------------------------------------------------------------------------
+// host: W = D^-1 K_gauss over design element centres (spacial.py:37-103)
+static int build_gauss(topt_filter* f, const double* c, const uint8_t* mask, double radius) {
+  const int64_t n = f->n_elem;
+  std::vector<int32_t> design;
+  design.reserve(n);
+  for (int64_t i = 0; i < n; ++i)
+    if (!mask || mask[i]) design.push_back((int32_t)i);
+  const int64_t nd = (int64_t)design.size();
+  if (nd == 0) return fail(TOPT_BAD_INPUT, "filter: empty design set");
+  const double s = radius / 3.0;
+  const double support = 3.0 * s;
+  const double sup2 = support * support;
+  // uniform grid hash of the design centres with cell size = support
+  double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+  for (int64_t k = 0; k < nd; ++k)
+    for (int d = 0; d < 3; ++d) {
+      const double v = c[d * n + design[k]];
+      lo[d] = std::min(lo[d], v);
+      hi[d] = std::max(hi[d], v);
+    }
+  const double h = support > 0 ? support : 1.0;
+  int64_t dim[3];
+  for (int d = 0; d < 3; ++d) dim[d] = std::max<int64_t>(1, (int64_t)std::floor((hi[d] - lo[d]) / h) + 1);
+  auto cell_of = [&](const double* p, int64_t out[3]) {
+    for (int d = 0; d < 3; ++d) {
+      int64_t q = (int64_t)std::floor((p[d] - lo[d]) / h);
+      out[d] = std::min<int64_t>(std::max<int64_t>(q, 0), dim[d] - 1);
+    }
+  };
+  const int64_t ncell = dim[0] * dim[1] * dim[2];
+  std::vector<int64_t> cptr(ncell + 1, 0);
+  std::vector<int64_t> ccell(nd);
+  for (int64_t k = 0; k < nd; ++k) {
+    double p[3] = {c[design[k]], c[n + design[k]], c[2 * n + design[k]]};
+    int64_t q[3];
+    cell_of(p, q);
+    ccell[k] = (q[2] * dim[1] + q[1]) * dim[0] + q[0];
+    cptr[ccell[k] + 1]++;
+  }
+  for (int64_t i = 0; i < ncell; ++i) cptr[i + 1] += cptr[i];
+  std::vector<int32_t> cidx(nd);
+  {
+    std::vector<int64_t> pos(cptr.begin(), cptr.end() - 1);
+    for (int64_t k = 0; k < nd; ++k) cidx[pos[ccell[k]]++] = (int32_t)k;
+  }
+  f->h_rowptr.assign(nd + 1, 0);
+  f->h_colind.clear();
+  f->h_vals.clear();
+  f->h_colind.reserve(nd * 20);
+  f->h_vals.reserve(nd * 20);
+  std::vector<std::pair<int32_t, double>> row;
+  for (int64_t k = 0; k < nd; ++k) {
+    const int64_t i = design[k];
+    const double pi[3] = {c[i], c[n + i], c[2 * n + i]};
+    int64_t q[3];
+    cell_of(pi, q);
+    row.clear();
+    for (int64_t z = std::max<int64_t>(q[2] - 1, 0); z <= std::min(q[2] + 1, dim[2] - 1); ++z)
+      for (int64_t y = std::max<int64_t>(q[1] - 1, 0); y <= std::min(q[1] + 1, dim[1] - 1); ++y)
+        for (int64_t x = std::max<int64_t>(q[0] - 1, 0); x <= std::min(q[0] + 1, dim[0] - 1); ++x) {
+          const int64_t cc = (z * dim[1] + y) * dim[0] + x;
+          for (int64_t m = cptr[cc]; m < cptr[cc + 1]; ++m) {
+            const int32_t kk = cidx[m];
+            const int64_t j = design[kk];
+            const double dx = c[j] - pi[0], dy = c[n + j] - pi[1], dz = c[2 * n + j] - pi[2];
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            if (d2 <= sup2) {
+              const double dij = std::sqrt(d2);
+              const double u = dij / s;
+              row.push_back({kk, std::exp(-0.5 * (u * u))});
+            }
+          }
+        }
+    std::sort(row.begin(), row.end(),
+              [](const std::pair<int32_t, double>& a, const std::pair<int32_t, double>& b) {
+                return a.first < b.first;
+              });
+    double rs = 0.0;
+    for (auto& pr : row) rs += pr.second;
+    if (rs == 0.0) rs = 1.0;
+    const double inv = 1.0 / rs;
+    for (auto& pr : row) {
+      f->h_colind.push_back(pr.first);
+      f->h_vals.push_back(pr.second * inv);
+    }
+    f->h_rowptr[k + 1] = (int32_t)f->h_colind.size();
+  }
+  f->n_design = nd;
+  f->nnz = (int64_t)f->h_colind.size();
+  // device copies with full-element columns, and the transpose
+  std::vector<int32_t> colfull(f->nnz);
+  for (int64_t k = 0; k < f->nnz; ++k) colfull[k] = design[f->h_colind[k]];
+  std::vector<int32_t> trp(nd + 1, 0), tcol(f->nnz);
+  std::vector<double> tval(f->nnz);
+  for (int64_t k = 0; k < f->nnz; ++k) trp[f->h_colind[k] + 1]++;
+  for (int64_t i = 0; i < nd; ++i) trp[i + 1] += trp[i];
+  {
+    std::vector<int32_t> pos(trp.begin(), trp.end() - 1);
+    for (int64_t r = 0; r < nd; ++r)
+      for (int32_t k = f->h_rowptr[r]; k < f->h_rowptr[r + 1]; ++k) {
+        const int32_t col = f->h_colind[k];
+        tcol[pos[col]] = design[r];
+        tval[pos[col]] = f->h_vals[k];
+        pos[col]++;
+      }
+  }
+  std::vector<int32_t> nondesign;
+  for (int64_t i = 0; i < n; ++i)
+    if (mask && !mask[i]) nondesign.push_back((int32_t)i);
+  f->n_nondesign = (int64_t)nondesign.size();
+  cudaStream_t st = nullptr;
+  int rc;
+  if ((rc = upload(f->design, design.data(), design.size(), st))) return rc;
+  if ((rc = upload(f->nondesign, nondesign.data(), nondesign.size(), st))) return rc;
+  if ((rc = upload(f->rowptr, f->h_rowptr.data(), f->h_rowptr.size(), st))) return rc;
+  if ((rc = upload(f->colfull, colfull.data(), colfull.size(), st))) return rc;
+  if ((rc = upload(f->vals, f->h_vals.data(), f->h_vals.size(), st))) return rc;
+  if ((rc = upload(f->t_rowptr, trp.data(), trp.size(), st))) return rc;
+  if ((rc = upload(f->t_colfull, tcol.data(), tcol.size(), st))) return rc;
+  if ((rc = upload(f->t_vals, tval.data(), tval.size(), st))) return rc;
+  if ((rc = f->cand.alloc(sizeof(double) * n))) return rc;
+  if ((rc = f->state.alloc(sizeof(OcState)))) return rc;
+  if ((rc = f->partials.alloc(sizeof(double) * f->sm * 16 * 2))) return rc;
+  if ((rc = f->counter.alloc(16 * sizeof(unsigned)))) return rc;
+  TOPT_CUDA(cudaMemset(f->counter.p, 0, 16 * sizeof(unsigned)));
+  TOPT_CUDA(cudaDeviceSynchronize());
+  return TOPT_OK;
+}
+
+// --------------------------------------------------------------------------
+// y[rows[i]] = sum_k V[k] x[col[k]]  (CSR rows indexed by design position)
+__global__ void k_csr_rows(int64_t nrows, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ col, const double* __restrict__ v,
+                           const int32_t* __restrict__ rows, const double* __restrict__ x,
+                           double* __restrict__ y) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nrows;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) s += v[k] * x[col[k]];
+    y[rows[i]] = s;
+  }
+}
+
+__global__ void k_scatter_copy(int64_t n, const int32_t* __restrict__ idx,
+                               const double* __restrict__ x, double* __restrict__ y,
+                               int zero) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t e = idx[i];
+    y[e] = zero ? 0.0 : x[e];
+  }
+}
+
+// --------------------------------------------------------------------------
+// Heaviside projection (projection.py:27-118)
+__global__ void k_projection(int64_t n, const double* __restrict__ x, double beta, double eta,
+                             double tbe, double den, double* __restrict__ h,
+                             double* __restrict__ dh) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double a = (x[i] - eta) * beta;
+    if (h) h[i] = (tbe + tanh(a)) / den;
+    if (dh) {
+      const double c = cosh(a);
+      dh[i] = (1.0 / (c * c)) * beta / den;
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// OC bisection (oc.py:16-95).  Step 1: candidate densities for the current
+// lmid; step 2: filter + projection + volume, then the bisection bookkeeping
+// in the last block (deterministic reduction order).
+__device__ __forceinline__ double clip_nan(double a, double lo, double hi) {
+  a = (a < lo) ? lo : a;   // NaN propagates like numpy.clip
+  return (a > hi) ? hi : a;
+}
+
+__global__ void k_oc_candidate(int64_t nd, const int32_t* __restrict__ design,
+                               const double* __restrict__ dc, double dc_scale,
+                               const double* __restrict__ rho_e,
+                               const OcState* __restrict__ st, topt_oc_params prm,
+                               double* __restrict__ cand, double* __restrict__ rho_new,
+                               double* __restrict__ scaling) {
+  TOPT_KERNEL_COUNT();
+  if (st->done) return;
+  const double lm = st->lmid;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t e = design[i];
+    double sr = (-(dc[e] / dc_scale)) / (lm + prm.eps);
+    sr = (prm.eta == 0.5) ? sqrt(sr) : pow(sr, prm.eta);
+    sr = clip_nan(sr, prm.scaling_min, prm.scaling_max);
+    const double r = rho_e[i];
+    const double lo = fmax(r - prm.move_limit, prm.rho_min);
+    const double hi = fmin(r + prm.move_limit, prm.rho_max);
+    const double v = clip_nan(r * sr, lo, hi);
+    cand[e] = v;
+    rho_new[i] = v;
+    if (scaling) scaling[i] = sr;
+  }
+}
+
+__global__ void k_gather(int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ x,
+                         double* __restrict__ y) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = x[idx[i]];
+}
+
+__global__ void k_scatter(int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ x,
+                          double* __restrict__ y) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[idx[i]] = x[i];
+}
+
+// Design-indexed reductions: OP 0 max |x[d]|, 1 max |x[d] - y[d]|,
+// 2 KKT: max over interior d of |x[d] + c * w[i]| (oc.py:230-240).
+template <int OP>
+__global__ void k_design_reduce(int64_t nd, const int32_t* __restrict__ design,
+                                const double* __restrict__ x, const double* __restrict__ y,
+                                const double* __restrict__ w, double c, double rho_min,
+                                double rho_max, double* partials, unsigned* counter,
+                                double* out) {
+  TOPT_KERNEL_COUNT();
+  double m = 0.0;
+  int nan = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t e = design[i];
+    double a;
+    if (OP == 0) a = fabs(x[e]);
+    else if (OP == 1) a = fabs(x[e] - y[e]);
+    else {
+      const double r = y[e];
+      if (!(r > rho_min + 1e-6 && r < rho_max - 1e-6)) continue;
+      a = fabs(x[e] + c * w[i]);
+    }
+    if (a != a) nan = 1;
+    m = a > m ? a : m;
+  }
+  __shared__ double shm[32];
+  __shared__ int anynan;
+  __shared__ bool last;
+  if (threadIdx.x == 0) anynan = 0;
+  __syncthreads();
+  if (nan) anynan = 1;
+  double v = warp_max(m);
+  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double u = threadIdx.x < (blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
+    u = warp_max(u);
+    if (threadIdx.x == 0) partials[blockIdx.x] = anynan ? NAN : u;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned t = atomicAdd(counter, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double r = 0.0;
+    bool bad = false;
+    for (unsigned b = 0; b < gridDim.x; ++b) {
+      const double pv = ((volatile double*)partials)[b];
+      if (pv != pv) bad = true;
+      r = pv > r ? pv : r;
+    }
+    *out = bad ? NAN : r;
+    *counter = 0u;
+  }
+}
+
+__global__ void k_oc_volume(int64_t nd, const int32_t* __restrict__ rowptr,
+                            const int32_t* __restrict__ col, const double* __restrict__ w,
+                            const double* __restrict__ cand, const double* __restrict__ vol,
+                            double vol_sum, topt_oc_params prm, double tbe, double den,
+                            OcState* st, double* partials, unsigned* counter) {
+  TOPT_KERNEL_COUNT();
+  if (st->done) return;
+  double acc[1] = {0.0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) s += w[k] * cand[col[k]];
+    const double a = (s - prm.beta_eta) * prm.beta;
+    const double hp = (tbe + tanh(a)) / den;
+    acc[0] += hp * vol[i];
+  }
+  __shared__ double sh[32];
+  __shared__ double total;
+  block_sum<double, 1>(acc, sh);
+  if (grid_finish<double, 1>(acc, partials, counter, &total)) {
+    if (threadIdx.x == 0) {
+      const double ve = total / vol_sum - prm.vol_frac;
+      st->vol_error = ve;
+      st->steps = st->it + 1;
+      if (fabs(ve) < prm.vol_tol || st->it >= prm.max_iter ||
+          fabs(st->l2 - st->l1) <= prm.tolerance) {
+        st->done = 1;
+      } else {
+        if (ve > 0) st->l1 = st->lmid;
+        else st->l2 = st->lmid;
+        st->it += 1;
+        st->lmid = 0.5 * (st->l1 + st->l2);
+      }
+    }
+  }
+}
+
+// --------------------------------------------------------------------------
+// Reductions with host results.
+template <int OP>  // 0: max |x| (NaN-propagating), 1: dot
+__global__ void k_reduce(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                         double* partials, unsigned* counter, double* out) {
+  TOPT_KERNEL_COUNT();
+  double acc[1] = {0.0};
+  bool nan = false;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (OP == 0) {
+      const double a = fabs(x[i]);
+      if (a != a) nan = true;
+      acc[0] = a > acc[0] ? a : acc[0];
+    } else {
+      acc[0] += x[i] * y[i];
+    }
+  }
+  if (OP == 0) {
+    __shared__ double shm[32];
+    __shared__ int anynan;
+    if (threadIdx.x == 0) anynan = 0;
+    __syncthreads();
+    if (nan) anynan = 1;
+    double v = warp_max(acc[0]);
+    if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      double u = threadIdx.x < (blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
+      u = warp_max(u);
+      if (threadIdx.x == 0) {
+        partials[blockIdx.x] = anynan ? NAN : u;
+      }
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+      __threadfence();
+      unsigned t = atomicAdd(counter, 1u);
+      last = (t == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      __threadfence();
+      double m = 0.0;
+      bool bad = false;
+      for (unsigned b = 0; b < gridDim.x; ++b) {
+        const double pv = ((volatile double*)partials)[b];
+        if (pv != pv) bad = true;
+        m = pv > m ? pv : m;
+      }
+      *out = bad ? NAN : m;
+      *counter = 0u;
+    }
+  } else {
+    __shared__ double sh[32];
+    block_sum<double, 1>(acc, sh);
+    grid_finish<double, 1>(acc, partials, counter, out);
+  }
+}
+
+// static scratch for the stand-alone reductions (one set per process/device)
+struct ReduceScratch {
+  DevBuf partials, counter, out;
+  int dev = -1;
+};
+static ReduceScratch g_red;
+
+static int reduce_scratch(int blocks) {
+  int dev = 0;
+  TOPT_CUDA(cudaGetDevice(&dev));
+  if (g_red.partials.p && g_red.dev == dev) return TOPT_OK;
+  int rc;
+  if ((rc = g_red.partials.alloc(sizeof(double) * blocks))) return rc;
+  if ((rc = g_red.counter.alloc(16 * sizeof(unsigned)))) return rc;
+  if ((rc = g_red.out.alloc(16 * sizeof(double)))) return rc;
+  TOPT_CUDA(cudaMemset(g_red.counter.p, 0, 16 * sizeof(unsigned)));
+  g_red.dev = dev;
+  return TOPT_OK;
+}
+
+}  // namespace topt
+
+using namespace topt;
+
+extern "C" {
+
+int topt_filter_gauss_create(int64_t n_elem, const double* centers, const uint8_t* design_mask,
+                             double radius, topt_filter** out) {
+  if (!out || !centers || n_elem <= 0 || !(radius > 0.0))
+    return fail(TOPT_BAD_INPUT, "filter_create: bad argument");
+  *out = nullptr;
+  std::unique_ptr<topt_filter> f(new (std::nothrow) topt_filter());
+  if (!f) return fail(TOPT_NO_MEMORY, "filter_create: host allocation");
+  f->n_elem = n_elem;
+  f->sm = device_sm_count();
+  int rc;
+  try {
+    rc = build_gauss(f.get(), centers, design_mask, radius);
+  } catch (const std::bad_alloc&) {
+    rc = fail(TOPT_NO_MEMORY, "filter_create: host allocation");
+  }
+  if (rc) return rc;
+  *out = f.release();
+  return TOPT_OK;
+}
+
+void topt_filter_destroy(topt_filter* f) {
+  if (!f) return;
+  cudaDeviceSynchronize();
+  delete f;
+}
+
+int topt_filter_set_stream(topt_filter* f, void* s) {
+  if (!f) return fail(TOPT_BAD_INPUT, "filter: null handle");
+  f->stream = (cudaStream_t)s;
+  return TOPT_OK;
+}
+
+int topt_filter_sizes(const topt_filter* f, int64_t* n_design, int64_t* nnz) {
+  if (!f) return fail(TOPT_BAD_INPUT, "filter: null handle");
+  if (n_design) *n_design = f->n_design;
+  if (nnz) *nnz = f->nnz;
+  return TOPT_OK;
+}
+
+int topt_filter_export(const topt_filter* f, int32_t* rowptr, int32_t* colind, double* vals) {
+  if (!f) return fail(TOPT_BAD_INPUT, "filter: null handle");
+  if (rowptr) std::copy(f->h_rowptr.begin(), f->h_rowptr.end(), rowptr);
+  if (colind) std::copy(f->h_colind.begin(), f->h_colind.end(), colind);
+  if (vals) std::copy(f->h_vals.begin(), f->h_vals.end(), vals);
+  return TOPT_OK;
+}
+
+int topt_filter_forward(topt_filter* f, const double* x, double* y) {
+  if (!f || !x || !y) return fail(TOPT_BAD_INPUT, "filter_forward: null argument");
+  if (x == y) return fail(TOPT_BAD_INPUT, "filter_forward: in-place call not supported");
+  const int g = grid_for(f->n_design, kFB, f->sm * 16);
+  k_csr_rows<<<g, kFB, 0, f->stream>>>(f->n_design, f->rowptr.as<int32_t>(),
+                                       f->colfull.as<int32_t>(), f->vals.as<double>(),
+                                       f->design.as<int32_t>(), x, y);
+  if (f->n_nondesign)
+    k_scatter_copy<<<grid_for(f->n_nondesign, kFB, f->sm * 16), kFB, 0, f->stream>>>(
+        f->n_nondesign, f->nondesign.as<int32_t>(), x, y, 0);
+  TOPT_CHECK_LAUNCH("filter_forward");
+  return TOPT_OK;
+}
+
+int topt_filter_gradient(topt_filter* f, const double* v, double* y) {
+  if (!f || !v || !y) return fail(TOPT_BAD_INPUT, "filter_gradient: null argument");
+  if (v == y) return fail(TOPT_BAD_INPUT, "filter_gradient: in-place call not supported");
+  const int g = grid_for(f->n_design, kFB, f->sm * 16);
+  k_csr_rows<<<g, kFB, 0, f->stream>>>(f->n_design, f->t_rowptr.as<int32_t>(),
+                                       f->t_colfull.as<int32_t>(), f->t_vals.as<double>(),
+                                       f->design.as<int32_t>(), v, y);
+  if (f->n_nondesign)
+    k_scatter_copy<<<grid_for(f->n_nondesign, kFB, f->sm * 16), kFB, 0, f->stream>>>(
+        f->n_nondesign, f->nondesign.as<int32_t>(), v, y, 1);
+  TOPT_CHECK_LAUNCH("filter_gradient");
+  return TOPT_OK;
+}
+
+int topt_projection(int64_t n, const double* x, double beta, double eta, double* h,
+                    double* dh, void* stream) {
+  if (n < 0 || (n > 0 && !x)) return fail(TOPT_BAD_INPUT, "projection: bad argument");
+  if (n == 0) return TOPT_OK;
+  const double tbe = std::tanh(beta * eta);
+  const double den = tbe + std::tanh(beta * (1.0 - eta)) + 1e-12;
+  k_projection<<<grid_for(n, kFB, device_sm_count() * 16), kFB, 0, (cudaStream_t)stream>>>(
+      n, x, beta, eta, tbe, den, h, dh);
+  TOPT_CHECK_LAUNCH("k_projection");
+  return TOPT_OK;
+}
+
+int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rho,
+                   const double* vol, double vol_sum, const topt_oc_params* prm,
+                   double* scaling, double* lmid, double* vol_error, int32_t* steps) {
+  if (!f || !dc || !rho || !vol || !prm) return fail(TOPT_BAD_INPUT, "oc_bisect: null argument");
+  if (!(prm->l1 < prm->l2)) return fail(TOPT_BAD_INPUT, "oc_bisect: need l1 < l2");
+  if (!(dc_scale > 0.0)) return fail(TOPT_BAD_INPUT, "oc_bisect: dc_scale must be > 0");
+  const int64_t nd = f->n_design;
+  int rc;
+  if (!f->rho_e.p && (rc = f->rho_e.alloc(sizeof(double) * nd))) return rc;
+  if (!f->rho_new.p && (rc = f->rho_new.alloc(sizeof(double) * nd))) return rc;
+  OcState s0{};
+  s0.l1 = prm->l1;
+  s0.l2 = prm->l2;
+  s0.lmid = 0.5 * (prm->l1 + prm->l2);
+  TOPT_CUDA(cudaMemcpyAsync(f->state.p, &s0, sizeof(s0), cudaMemcpyHostToDevice, f->stream));
+  const double tbe = std::tanh(prm->beta * prm->beta_eta);
+  const double den = tbe + std::tanh(prm->beta * (1.0 - prm->beta_eta)) + 1e-12;
+  // every step halves |l2 - l1|; the loop ends once it is <= tolerance
+  int max_steps = 1;
+  {
+    double w = prm->l2 - prm->l1;
+    while (w > prm->tolerance && max_steps < 4096) { w *= 0.5; ++max_steps; }
+    max_steps = std::min(max_steps + 1, prm->max_iter + 1);
+  }
+  const int g = grid_for(nd, kFB, f->sm * 8);
+  const int32_t* design = f->design.as<int32_t>();
+  k_gather<<<g, kFB, 0, f->stream>>>(nd, design, rho, f->rho_e.as<double>());
+  OcState* st = f->state.as<OcState>();
+  for (int k = 0; k < max_steps; ++k) {
+    k_oc_candidate<<<g, kFB, 0, f->stream>>>(nd, design, dc, dc_scale, f->rho_e.as<double>(),
+                                             st, *prm, f->cand.as<double>(),
+                                             f->rho_new.as<double>(), scaling);
+    k_oc_volume<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(), f->colfull.as<int32_t>(),
+                                          f->vals.as<double>(), f->cand.as<double>(), vol,
+                                          vol_sum, *prm, tbe, den, st,
+                                          f->partials.as<double>(), f->counter.as<unsigned>());
+  }
+  k_scatter<<<g, kFB, 0, f->stream>>>(nd, design, f->rho_new.as<double>(), rho);
+  TOPT_CHECK_LAUNCH("oc_bisect");
+  OcState out{};
+  TOPT_CUDA(cudaMemcpyAsync(&out, f->state.p, sizeof(out), cudaMemcpyDeviceToHost, f->stream));
+  TOPT_CUDA(cudaStreamSynchronize(f->stream));
+  if (lmid) *lmid = out.lmid;
+  if (vol_error) *vol_error = out.vol_error;
+  if (steps) *steps = out.steps;
+  if (!out.done) return fail(TOPT_MAXITER, "oc_bisect: bisection did not terminate");
+  return TOPT_OK;
+}
+
+int topt_design_reduce(topt_filter* f, int32_t op, const double* x, const double* y,
+                       const double* w, double c, double rho_min, double rho_max,
+                       double* out) {
+  if (!f || !x || !out || op < 0 || op > 2 || (op > 0 && !y) || (op == 2 && !w))
+    return fail(TOPT_BAD_INPUT, "design_reduce: bad argument");
+  const int64_t nd = f->n_design;
+  const int g = grid_for(nd, kFB, f->sm * 8);
+  double* part = f->partials.as<double>();
+  unsigned* ctr = f->counter.as<unsigned>() + 1;
+  double* res = f->partials.as<double>() + f->sm * 16 * 2 - 1;
+  const int32_t* design = f->design.as<int32_t>();
+  if (op == 0)
+    k_design_reduce<0><<<g, kFB, 0, f->stream>>>(nd, design, x, y, w, c, rho_min, rho_max, part,
+                                                 ctr, res);
+  else if (op == 1)
+    k_design_reduce<1><<<g, kFB, 0, f->stream>>>(nd, design, x, y, w, c, rho_min, rho_max, part,
+                                                 ctr, res);
+  else
+    k_design_reduce<2><<<g, kFB, 0, f->stream>>>(nd, design, x, y, w, c, rho_min, rho_max, part,
+                                                 ctr, res);
+  TOPT_CHECK_LAUNCH("k_design_reduce");
+  TOPT_CUDA(cudaMemcpyAsync(out, res, sizeof(double), cudaMemcpyDeviceToHost, f->stream));
+  TOPT_CUDA(cudaStreamSynchronize(f->stream));
+  return TOPT_OK;
+}
+
+int topt_reduce_max_abs(int64_t n, const double* x, double* out, void* stream) {
+  if (!out || n < 0 || (n > 0 && !x)) return fail(TOPT_BAD_INPUT, "reduce_max_abs: bad argument");
+  if (n == 0) { *out = 0.0; return TOPT_OK; }
+  const int blocks = grid_for(n, kFB, device_sm_count() * 8);
+  int rc = reduce_scratch(device_sm_count() * 8);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_reduce<0><<<blocks, kFB, 0, s>>>(n, x, nullptr, g_red.partials.as<double>(),
+                                     g_red.counter.as<unsigned>(), g_red.out.as<double>());
+  TOPT_CHECK_LAUNCH("k_reduce<max>");
+  TOPT_CUDA(cudaMemcpyAsync(out, g_red.out.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  TOPT_CUDA(cudaStreamSynchronize(s));
+  return TOPT_OK;
+}
+
+int topt_reduce_dot(int64_t n, const double* x, const double* y, double* out, void* stream) {
+  if (!out || n < 0 || (n > 0 && (!x || !y))) return fail(TOPT_BAD_INPUT, "reduce_dot: bad argument");
+  if (n == 0) { *out = 0.0; return TOPT_OK; }
+  const int blocks = grid_for(n, kFB, device_sm_count() * 8);
+  int rc = reduce_scratch(device_sm_count() * 8);
+  if (rc) return rc;
+  cudaStream_t s = (cudaStream_t)stream;
+  k_reduce<1><<<blocks, kFB, 0, s>>>(n, x, y, g_red.partials.as<double>(),
+                                     g_red.counter.as<unsigned>() + 1, g_red.out.as<double>() + 1);
+  TOPT_CHECK_LAUNCH("k_reduce<dot>");
+  TOPT_CUDA(cudaMemcpyAsync(out, g_red.out.as<double>() + 1, sizeof(double),
+                            cudaMemcpyDeviceToHost, s));
+  TOPT_CUDA(cudaStreamSynchronize(s));
+  return TOPT_OK;
+}
+
+}  // extern "C"
+
+namespace topt {
+int launches_filter(unsigned long long* out) {
+  TOPT_CUDA(cudaMemcpyFromSymbol(out, g_kernel_launches, sizeof(unsigned long long)));
+  return TOPT_OK;
+}
+}  // namespace topt

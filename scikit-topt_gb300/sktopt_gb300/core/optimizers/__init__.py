@@ -1,0 +1,5 @@
+from .common_density import DensityMethod, DensityMethodConfig, DensityMethod_OC_Config
+from .oc import OC_Config, OC_Optimizer
+
+__all__ = ["DensityMethod", "DensityMethodConfig", "DensityMethod_OC_Config", "OC_Config",
+           "OC_Optimizer"]

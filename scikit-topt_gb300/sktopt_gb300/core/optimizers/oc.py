@@ -1,0 +1,77 @@
+"""OC optimizer with the GPU bisection.
+
+Drop-in for ``OC_Optimizer`` / ``OC_Config`` (sktopt/core/optimizers/oc.py:
+98-250): sensitivity normalisation by max |dC| (or a percentile) with the 0.6
+EMA from iteration 2 on, the bisection on the volume multiplier in
+[lambda_lower, lambda_upper] with every candidate filtered and projected
+(``bisection_with_physical_volume`` oc.py:16-95, max_iter 1000, tolerance
+1e-5, vol_tol 1e-4), and the KKT infinity norm over interior elements.
+The whole bisection runs on the device (``topt_oc_bisect``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import Literal
+
+import numpy as np
+
+from ... import _native as N
+from ... import tools
+from ..._device import stream_handle
+from .common_density import DensityMethod, DensityMethod_OC_Config
+
+
+@dataclass
+class OC_Config(DensityMethod_OC_Config):
+    interpolation: Literal["SIMP"] = "SIMP"
+    eta: tools.SchedulerConfig = field(
+        default_factory=lambda: tools.SchedulerConfig.constant(target_value=0.5))
+    scaling_rate_min: float = 0.7
+    scaling_rate_max: float = 1.3
+    sensitivity_scale_floor: float = 1e-12
+
+
+class OC_Optimizer(DensityMethod):
+    def __init__(self, cfg: OC_Config, tsk, device=None):
+        assert cfg.lambda_lower < cfg.lambda_upper
+        super().__init__(cfg, tsk, device)
+        self.recorder.add("-dC")
+        self.recorder.add("lmid")
+        self.running_scale = 0.0
+        self.last_bisection_steps = 0
+
+    def rho_update(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
+        cfg = self.cfg
+        flt = self.filter
+        if isinstance(percentile, float):
+            scale = flt.design_percentile_abs(st.dC_drho_full, percentile)
+        else:
+            scale = flt.design_reduce(0, st.dC_drho_full)
+        scale = max(scale, cfg.sensitivity_scale_floor)
+        self.running_scale = 0.6 * self.running_scale + (1 - 0.6) * scale \
+            if iter_num > 1 else scale
+        prm = N.OcParams(rho_min=cfg.rho_min, rho_max=cfg.rho_max, move_limit=move_limit,
+                         eta=eta, eps=1e-12, vol_frac=vol_frac, beta=beta,
+                         beta_eta=cfg.beta_eta, scaling_min=cfg.scaling_rate_min,
+                         scaling_max=cfg.scaling_rate_max, vol_tol=1e-4,
+                         l1=cfg.lambda_lower, l2=cfg.lambda_upper, tolerance=1e-5,
+                         max_iter=1000)
+        lmid, verr, steps = C.c_double(), C.c_double(), C.c_int32()
+        flt._bind()
+        N.check(N.load().topt_oc_bisect(
+            flt.h, C.c_void_p(st.dC_drho_full.data_ptr()), float(self.running_scale),
+            C.c_void_p(st.rho.data_ptr()), C.c_void_p(self._vol_design.data_ptr()),
+            self._vol_design_sum, C.byref(prm), C.c_void_p(st.scaling_rate.data_ptr()),
+            C.byref(lmid), C.byref(verr), C.byref(steps)))
+        # KKT over interior design elements: |dC_raw + lmid * scale * dV| (oc.py:230-240)
+        self.kkt_residual = flt.design_reduce(2, st.dC_drho_full, st.rho,
+                                              w=self._dV_drho_design,
+                                              c=lmid.value * self.running_scale,
+                                              rho_min=cfg.rho_min, rho_max=cfg.rho_max)
+        st.vol_error = verr.value
+        st.kkt_residual = self.kkt_residual
+        self.last_bisection_steps = steps.value
+        self.recorder.feed_data("lmid", lmid.value)
+        self.recorder.feed_data("vol_error", verr.value)
+        self.recorder.feed_data("kkt_residual", self.kkt_residual)

@@ -1,0 +1,190 @@
+"""Python handle around the native FEM engine (topt_fem_* in include/topt.h)."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .. import _native as N
+from .._device import as_device, default_device, stream_handle
+from ..mesh.grid import GridMesh
+
+
+@dataclass
+class SolveStats:
+    status: int
+    iters: int
+    outer: int
+    relres: float
+
+    @property
+    def status_name(self) -> str:
+        return N.STATUS_NAMES.get(self.status, str(self.status))
+
+
+class FemEngine:
+    """Pattern, operator, hierarchy and PCG for one mesh / DOF layout.
+
+    bs = 3 (elasticity) or 1 (conduction).  ``ke`` holds unit-modulus element
+    matrices: one shared (1, nd, nd) or one per element (n_e, nd, nd).
+    """
+
+    def __init__(self, mesh: GridMesh, bs: int, ke: np.ndarray, dirichlet_mask: np.ndarray,
+                 mixed: bool = False, multigrid: bool = True, mg_levels: int = 16,
+                 mg_coarse_max: int = 200, device=None):
+        self.lib = N.load()
+        self.device = device or default_device()
+        self.mesh = mesh
+        self.bs = bs
+        self.nloc = mesh.t.shape[0]
+        self.n_dof = bs * mesh.nnodes
+        self.mixed = bool(mixed)
+        ke = np.ascontiguousarray(ke, dtype=np.float64)
+        if ke.ndim == 2:
+            ke = ke[None]
+        self._t = np.ascontiguousarray(mesh.t, dtype=np.int32)
+        self._ke = ke
+        self._mask = np.ascontiguousarray(dirichlet_mask, dtype=np.uint8)
+        self._ijk = np.ascontiguousarray(mesh.node_ijk, dtype=np.int32)
+        self._cell = np.ascontiguousarray(mesh.cell_of_elem, dtype=np.int32)
+        d = N.FemDesc()
+        d.bs = bs
+        d.nloc = self.nloc
+        d.n_nodes = mesh.nnodes
+        d.n_elem = mesh.nelements
+        d.t = self._t.ctypes.data_as(C.POINTER(C.c_int32))
+        d.ke = ke.ctypes.data_as(C.POINTER(C.c_double))
+        d.n_ke = ke.shape[0]
+        d.dirichlet = self._mask.ctypes.data_as(C.POINTER(C.c_uint8))
+        if multigrid:
+            d.grid[:] = list(mesh.shape)
+            d.node_ijk = self._ijk.ctypes.data_as(C.POINTER(C.c_int32))
+            d.cell_of_elem = (self._cell.ctypes.data_as(C.POINTER(C.c_int32))
+                              if mesh.kind != "hex" else None)
+        d.mixed = 1 if mixed else 0
+        d.mg_levels = mg_levels if multigrid else 1
+        d.mg_coarse_max = mg_coarse_max
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            N.check(self.lib.topt_fem_create(C.byref(d), C.byref(h)))
+        self.h = h
+        nd, nnzb, nlev = C.c_int64(), C.c_int64(), C.c_int32()
+        N.check(self.lib.topt_fem_sizes(self.h, C.byref(nd), C.byref(nnzb), C.byref(nlev)))
+        self.nnzb = nnzb.value
+        self.n_levels = nlev.value
+        self.multigrid = self.n_levels > 1
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.topt_fem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _bind(self):
+        N.check(self.lib.topt_fem_set_stream(self.h, C.c_void_p(stream_handle())))
+
+    def update(self, rho: torch.Tensor, E0: float, Emin: float, p: float):
+        """coef = SIMP(rho); K = sum coef Ke; enforce; refresh the preconditioner."""
+        self._bind()
+        rho = as_device(rho, device=self.device)
+        N.check(self.lib.topt_fem_update(self.h, C.c_void_p(rho.data_ptr()), float(E0),
+                                         float(Emin), float(p)))
+
+    def solve(self, F: torch.Tensor, U: torch.Tensor, method: int, precond: int, rtol: float,
+              maxiter: int, inner_rtol: float = 1e-4, max_outer: int = 20,
+              cheb_degree: int = 2, check_every: int = 1, raise_on_maxiter=False):
+        """Solve K_e U = F_e for every column; returns (compliance, SolveStats)."""
+        self._bind()
+        L = F.shape[1] if F.dim() == 2 else 1
+        o = N.SolveOpts(method=method, precond=precond, rtol=rtol, maxiter=maxiter,
+                        inner_rtol=inner_rtol, max_outer=max_outer,
+                        cheb_degree=cheb_degree, check_every=check_every)
+        info = N.SolveInfo()
+        comp = np.zeros(L)
+        N.check(self.lib.topt_fem_solve(self.h, C.c_void_p(F.data_ptr()),
+                                        C.c_void_p(U.data_ptr()), L, C.byref(o),
+                                        C.byref(info), comp.ctypes.data_as(C.c_void_p)))
+        st = SolveStats(info.status, info.iters, info.outer, info.relres)
+        if info.status == N.TOPT_NONFINITE or (raise_on_maxiter and info.status != N.TOPT_OK):
+            raise N.ToptError(info.status, f"linear solve failed: {st}")
+        return comp, st
+
+    def spmv(self, x: torch.Tensor, dtype=torch.float64) -> torch.Tensor:
+        self._bind()
+        L = x.shape[1] if x.dim() == 2 else 1
+        y = torch.empty_like(x)
+        code = N.TOPT_F64 if dtype == torch.float64 else N.TOPT_F32
+        N.check(self.lib.topt_fem_spmv(self.h, code, C.c_void_p(x.data_ptr()),
+                                       C.c_void_p(y.data_ptr()), L))
+        return y
+
+    def export_values(self) -> torch.Tensor:
+        self._bind()
+        v = torch.empty(self.nnzb * self.bs * self.bs, dtype=torch.float64, device=self.device)
+        N.check(self.lib.topt_fem_export_values(self.h, C.c_void_p(v.data_ptr())))
+        return v
+
+    def energy(self, U: torch.Tensor, rho: torch.Tensor, E0, Emin, p, dh=None,
+               want_energy=True, want_dc=False):
+        """Element energies (n_e, L) and dC_drho_simp * dh (n_e, L)."""
+        self._bind()
+        L = U.shape[1] if U.dim() == 2 else 1
+        ne = self.mesh.nelements
+        en = torch.empty((ne, L), dtype=torch.float64, device=self.device) if want_energy else None
+        dc = torch.empty((ne, L), dtype=torch.float64, device=self.device) if want_dc else None
+        N.check(self.lib.topt_fem_energy(
+            self.h, C.c_void_p(U.data_ptr()), L, C.c_void_p(rho.data_ptr()), float(E0),
+            float(Emin), float(p), C.c_void_p(dh.data_ptr()) if dh is not None else None,
+            C.c_void_p(en.data_ptr()) if en is not None else None,
+            C.c_void_p(dc.data_ptr()) if dc is not None else None))
+        return en, dc
+
+
+def pattern(mesh: GridMesh):
+    """Host pattern (rowptr, colind, cptr, contrib) of a mesh, via the native builder."""
+    lib = N.load()
+    t = np.ascontiguousarray(mesh.t, dtype=np.int32)
+    h = C.c_void_p()
+    N.check(lib.topt_pattern_build(mesh.nnodes, mesh.nelements, t.shape[0],
+                                   t.ctypes.data_as(C.c_void_p), C.byref(h)))
+    try:
+        nnzb, nc = C.c_int64(), C.c_int64()
+        N.check(lib.topt_pattern_sizes(h, C.byref(nnzb), C.byref(nc)))
+        rowptr = np.empty(mesh.nnodes + 1, np.int32)
+        colind = np.empty(nnzb.value, np.int32)
+        cptr = np.empty(nnzb.value + 1, np.int64)
+        contrib = np.empty(nc.value, np.int32)
+        N.check(lib.topt_pattern_export(h, rowptr.ctypes.data_as(C.c_void_p),
+                                        colind.ctypes.data_as(C.c_void_p),
+                                        cptr.ctypes.data_as(C.c_void_p),
+                                        contrib.ctypes.data_as(C.c_void_p)))
+    finally:
+        lib.topt_pattern_free(h)
+    return rowptr, colind, cptr, contrib
+
+
+def block_to_scalar_csr(rowptr, colind, vals, bs):
+    """Scalar CSR (indptr, indices, data) with interleaved DOFs bs*node + comp
+    from a node pattern and its (nnzb, bs, bs) block values."""
+    rowptr = np.asarray(rowptr, np.int64)
+    colind = np.asarray(colind, np.int64)
+    nnzb = colind.size
+    n = rowptr.size - 1
+    brow = np.repeat(np.arange(n), np.diff(rowptr))
+    k, c, d = np.meshgrid(np.arange(nnzb), np.arange(bs), np.arange(bs), indexing="ij")
+    k, c, d = k.ravel(), c.ravel(), d.ravel()
+    order = np.lexsort((d, k, brow[k] * bs + c))
+    k, c, d = k[order], c[order], d[order]
+    indices = bs * colind[k] + d
+    data = np.asarray(vals).reshape(nnzb, bs, bs)[k, c, d]
+    counts = np.repeat(np.diff(rowptr) * bs, bs)
+    indptr = np.zeros(n * bs + 1, np.int64)
+    indptr[1:] = np.cumsum(counts)
+    return indptr, indices, data

@@ -1,0 +1,190 @@
+"""Meshes on a logical cell grid: structured hexahedra or 6-tet splits.
+
+Node and element numbering follow scikit-fem's ``MeshHex.init_tensor`` (used
+by sktopt/mesh/toy_problem.py:10-37): node (ix, iy, iz) has index
+``iy + (ny+1)*(ix + (nx+1)*iz)`` and cell (ex, ey, ez) index
+``ey + ny*(ex + nx*ez)``; the eight local hex nodes are the offsets
+(0,0,0) (0,1,0) (1,0,0) (0,0,1) (1,1,0) (0,1,1) (1,0,1) (1,1,1).  The logical
+coordinates are kept so the multigrid preconditioner can coarsen the grid.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+HEX_OFFSETS = np.array([[0, 0, 0], [0, 1, 0], [1, 0, 0], [0, 0, 1],
+                        [1, 1, 0], [0, 1, 1], [1, 0, 1], [1, 1, 1]], dtype=np.int64)
+
+# Freudenthal split of a cell into 6 tets, one per axis order of the path
+# (0,0,0) -> (1,1,1); conforming between neighbouring cells.
+TET_AXIS_ORDERS = ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0))
+
+
+class GridMesh:
+    """skfem-shaped mesh: ``p`` (3, n_nodes), ``t`` (nloc, n_elem)."""
+
+    def __init__(self, p, t, kind, shape, node_ijk, cell_of_elem):
+        self.p = np.ascontiguousarray(p, dtype=np.float64)
+        self.t = np.ascontiguousarray(t, dtype=np.int64)
+        self.kind = kind
+        self.shape = tuple(int(s) for s in shape)
+        self.node_ijk = np.ascontiguousarray(node_ijk, dtype=np.int64)
+        self.cell_of_elem = np.ascontiguousarray(cell_of_elem, dtype=np.int64)
+
+    @property
+    def nnodes(self) -> int:
+        return self.p.shape[1]
+
+    @property
+    def nelements(self) -> int:
+        return self.t.shape[1]
+
+    @property
+    def nvertices(self) -> int:
+        return self.p.shape[1]
+
+
+def _node_ijk(nx, ny, nz):
+    n = np.arange((nx + 1) * (ny + 1) * (nz + 1), dtype=np.int64)
+    iy = n % (ny + 1)
+    ix = (n // (ny + 1)) % (nx + 1)
+    iz = n // ((ny + 1) * (nx + 1))
+    return np.vstack([ix, iy, iz])
+
+
+def _cell_ijk(nx, ny, nz):
+    c = np.arange(nx * ny * nz, dtype=np.int64)
+    ey = c % ny
+    ex = (c // ny) % nx
+    ez = c // (ny * nx)
+    return ex, ey, ez
+
+
+def _nid(ix, iy, iz, nx, ny):
+    return iy + (ny + 1) * (ix + (nx + 1) * iz)
+
+
+def _orient_hex(t, p):
+    """sktopt/mesh/utils.py:18-54: swap local nodes 1 and 3 on negative orientation."""
+    c = p[:, t]
+    det = np.einsum("ij,ij->j", np.cross((c[:, 1] - c[:, 0]).T, (c[:, 3] - c[:, 0]).T).T,
+                    c[:, 4] - c[:, 0])
+    bad = det < 0
+    if np.any(bad):
+        t = t.copy()
+        a = t[1, bad].copy()
+        t[1, bad] = t[3, bad]
+        t[3, bad] = a
+    return t
+
+
+def _orient_tet(t, p):
+    """sktopt/mesh/utils.py:57-91: swap local nodes 1 and 2 on negative volume."""
+    c = p[:, t]
+    vol = np.einsum("ij,ij->j", np.cross((c[:, 1] - c[:, 0]).T, (c[:, 2] - c[:, 0]).T).T,
+                    c[:, 3] - c[:, 0])
+    bad = vol < 0
+    if np.any(bad):
+        t = t.copy()
+        a = t[1, bad].copy()
+        t[1, bad] = t[2, bad]
+        t[2, bad] = a
+    return t
+
+
+def structured_hex(x, y, z) -> GridMesh:
+    """Hex mesh on the tensor grid of node coordinates x, y, z."""
+    x, y, z = (np.asarray(v, dtype=np.float64) for v in (x, y, z))
+    nx, ny, nz = len(x) - 1, len(y) - 1, len(z) - 1
+    ijk = _node_ijk(nx, ny, nz)
+    p = np.vstack([x[ijk[0]], y[ijk[1]], z[ijk[2]]])
+    ex, ey, ez = _cell_ijk(nx, ny, nz)
+    t = np.empty((8, ex.size), dtype=np.int64)
+    for a, (ox, oy, oz) in enumerate(HEX_OFFSETS):
+        t[a] = _nid(ex + ox, ey + oy, ez + oz, nx, ny)
+    t = _orient_hex(t, p)
+    return GridMesh(p, t, "hex", (nx, ny, nz), ijk, np.arange(ex.size))
+
+
+def create_box_hex(nx, ny, nz, hx=1.0, hy=1.0, hz=1.0) -> GridMesh:
+    return structured_hex(np.arange(nx + 1) * float(hx), np.arange(ny + 1) * float(hy),
+                          np.arange(nz + 1) * float(hz))
+
+
+def create_box_hex_len(x_len, y_len, z_len, mesh_size) -> GridMesh:
+    """sktopt/mesh/toy_problem.py:10-37."""
+    n = [int(np.ceil(v / mesh_size)) for v in (x_len, y_len, z_len)]
+    return structured_hex(np.linspace(0, x_len, n[0] + 1), np.linspace(0, y_len, n[1] + 1),
+                          np.linspace(0, z_len, n[2] + 1))
+
+
+def create_box_tet(nx, ny, nz, lx, ly, lz, jitter=0.0, seed=0) -> GridMesh:
+    """6-tet split of an nx x ny x nz grid on [0,lx]x[0,ly]x[0,lz].
+
+    Interior node coordinates move by U(-jitter*h, jitter*h) per axis
+    (``numpy.random.default_rng(seed)``); boundary coordinates stay on their
+    faces.
+    """
+    hx, hy, hz = lx / nx, ly / ny, lz / nz
+    ijk = _node_ijk(nx, ny, nz)
+    p = np.vstack([ijk[0] * hx, ijk[1] * hy, ijk[2] * hz]).astype(np.float64)
+    if jitter > 0.0:
+        rng = np.random.default_rng(seed)
+        d = rng.uniform(-1.0, 1.0, size=p.shape)
+        h = np.array([hx, hy, hz])[:, None]
+        n = np.array([nx, ny, nz])[:, None]
+        inside = (ijk > 0) & (ijk < n)
+        p = p + np.where(inside, d * jitter * h, 0.0)
+    ex, ey, ez = _cell_ijk(nx, ny, nz)
+    nc = ex.size
+    t = np.empty((4, 6 * nc), dtype=np.int64)
+    for k, order in enumerate(TET_AXIS_ORDERS):
+        off = [0, 0, 0]
+        t[0, k::6] = _nid(ex, ey, ez, nx, ny)
+        for a, ax in enumerate(order):
+            off[ax] += 1
+            t[a + 1, k::6] = _nid(ex + off[0], ey + off[1], ez + off[2], nx, ny)
+    t = _orient_tet(t, p)
+    return GridMesh(p, t, "tet", (nx, ny, nz), ijk, np.repeat(np.arange(nc), 6))
+
+
+def elements_volume(mesh: GridMesh) -> np.ndarray:
+    """sktopt/fea/composer.py:164-180 (tet) and 191-248 (hex, six |tet| volumes)."""
+    c = mesh.p[:, mesh.t]
+
+    def tet(a, b, cc, d, signed=False):
+        v = np.einsum("ij,ij->j", np.cross((c[:, b] - c[:, a]).T, (c[:, cc] - c[:, a]).T).T,
+                      c[:, d] - c[:, a]) / 6.0
+        return v if signed else np.abs(v)
+
+    if mesh.kind == "tet":
+        v = tet(0, 1, 2, 3, signed=True)
+        if np.any(v < -1e-12):
+            raise ValueError("negative tet volume")
+        return v
+    out = np.zeros(mesh.nelements)
+    for q in ((0, 1, 3, 4), (1, 2, 3, 6), (1, 5, 6, 4), (3, 6, 7, 4), (1, 3, 6, 4),
+              (1, 6, 5, 4)):
+        out += tet(*q)
+    return out
+
+
+def element_centers(mesh: GridMesh) -> np.ndarray:
+    """sktopt/filters/spacial.py:13-16."""
+    return np.mean(mesh.p[:, mesh.t], axis=1)
+
+
+def get_elements_by_nodes(mesh: GridMesh, target_nodes) -> np.ndarray:
+    """sktopt/mesh/utils.py:180-228: sorted elements touching any target node."""
+    if isinstance(target_nodes, np.ndarray):
+        nodes = np.unique(target_nodes)
+    else:
+        nodes = np.unique(np.concatenate([np.asarray(n).ravel() for n in target_nodes]))
+    hit = np.zeros(mesh.nnodes, dtype=bool)
+    hit[nodes.astype(np.int64)] = True
+    return np.nonzero(hit[mesh.t].any(axis=0))[0].astype(np.int32)
+
+
+def setdiff1d(a, b):
+    """sktopt/mesh/task_common.py:18-21."""
+    a = np.asarray(a)
+    return np.ascontiguousarray(a[~np.isin(a, b)])

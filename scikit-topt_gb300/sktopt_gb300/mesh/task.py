@@ -1,0 +1,134 @@
+"""Problem definitions: boundary sets, design sets and loads.
+
+Mirrors ``FEMDomain.from_nodes`` (sktopt/mesh/task_common.py:105-270),
+``exlude_dirichlet_from_design`` (task_common.py:398-401), ``LinearElasticity``
+(sktopt/mesh/task_elastic.py:85-147) and ``LinearHeatConduction``
+(sktopt/mesh/task_heat.py:142-321): elements touching load nodes leave the
+design set, elements touching Dirichlet nodes leave it when the optimizer's
+``design_dirichlet`` is False, and DOFs are interleaved ``bs*node + comp``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .grid import GridMesh, elements_volume, get_elements_by_nodes, setdiff1d
+
+_COMP = {"u^1": 0, "u^2": 1, "u^3": 2}
+
+
+@dataclass
+class FEMDomain:
+    mesh: GridMesh
+    dirichlet_nodes: np.ndarray
+    dirichlet_dofs: np.ndarray
+    dirichlet_elements: np.ndarray
+    neumann_nodes: np.ndarray | list | None
+    neumann_elements: np.ndarray
+    design_elements: np.ndarray
+    free_dofs: np.ndarray
+    all_elements: np.ndarray
+    fixed_elements: np.ndarray
+    dirichlet_neumann_elements: np.ndarray
+    elements_volume: np.ndarray
+    bs: int = 3
+
+    @property
+    def design_mask(self) -> np.ndarray:
+        return np.isin(self.all_elements, self.design_elements)
+
+    @property
+    def n_dof(self) -> int:
+        return self.bs * self.mesh.nnodes
+
+    @property
+    def dirichlet_mask(self) -> np.ndarray:
+        m = np.zeros(self.n_dof, dtype=np.uint8)
+        m[self.dirichlet_dofs] = 1
+        return m
+
+    def exlude_dirichlet_from_design(self):
+        """task_common.py:398-401."""
+        self.design_elements = setdiff1d(self.design_elements, self.dirichlet_elements)
+
+    @staticmethod
+    def _sets(mesh, bs, dirichlet_nodes, dirichlet_dir, neumann_nodes, design_elements):
+        dn = np.unique(np.asarray(dirichlet_nodes, dtype=np.int64))
+        if dirichlet_dir == "all" or bs == 1:
+            comps = np.arange(bs)
+        else:
+            comps = np.array([_COMP[dirichlet_dir]])
+        ddofs = np.sort((bs * dn[:, None] + comps[None, :]).ravel())
+        dir_el = get_elements_by_nodes(mesh, [dn])
+        if neumann_nodes is not None:
+            nn = neumann_nodes if isinstance(neumann_nodes, list) else [neumann_nodes]
+            neu_el = get_elements_by_nodes(mesh, nn)
+            if neu_el.size == 0:
+                raise ValueError("neumann_elements has not been set.")
+        else:
+            neu_el = np.array([], dtype=np.int32)
+        design = setdiff1d(np.asarray(design_elements), neu_el)
+        if design.size == 0:
+            raise ValueError("design_elements is empty")
+        all_el = np.arange(mesh.nelements)
+        fixed = setdiff1d(all_el, design)
+        dn_el = np.concatenate([v for v in (dir_el, neu_el) if v.size > 0]) \
+            if (dir_el.size + neu_el.size) else np.array([], dtype=np.int64)
+        free = setdiff1d(np.arange(bs * mesh.nnodes), ddofs)
+        return dict(dirichlet_nodes=dn, dirichlet_dofs=ddofs, dirichlet_elements=dir_el,
+                    neumann_elements=neu_el, design_elements=design, free_dofs=free,
+                    all_elements=all_el, fixed_elements=fixed,
+                    dirichlet_neumann_elements=dn_el,
+                    elements_volume=elements_volume(mesh))
+
+
+@dataclass
+class LinearElasticity(FEMDomain):
+    E: float = 1.0
+    nu: float = 0.3
+    neumann_linear: list = field(default_factory=list)
+
+    @property
+    def material_coef(self) -> float:
+        return self.E
+
+    @property
+    def n_tasks(self) -> int:
+        return len(self.neumann_linear)
+
+    @classmethod
+    def from_nodes(cls, mesh, dirichlet_nodes, dirichlet_dir, neumann_nodes,
+                   neumann_linear, design_elements, E, nu):
+        """task_common.py:105-270 with nodal load vectors (one per load case)."""
+        s = FEMDomain._sets(mesh, 3, dirichlet_nodes, dirichlet_dir, neumann_nodes,
+                            design_elements)
+        loads = neumann_linear if isinstance(neumann_linear, list) else [neumann_linear]
+        loads = [np.ascontiguousarray(f, dtype=np.float64) for f in loads]
+        return cls(mesh=mesh, neumann_nodes=neumann_nodes, bs=3, E=float(E), nu=float(nu),
+                   neumann_linear=loads, **s)
+
+
+@dataclass
+class LinearHeatConduction(FEMDomain):
+    k: float = 1.0
+    dirichlet_values: float = 0.0
+    emit: np.ndarray | None = None
+    objective: str = "compliance"
+
+    @property
+    def material_coef(self) -> float:
+        return self.k
+
+    @property
+    def n_tasks(self) -> int:
+        return 1
+
+    @classmethod
+    def from_nodes(cls, mesh, dirichlet_nodes, emit, design_elements, k=1.0,
+                   dirichlet_values=0.0):
+        """task_heat.py:142-321 with a volumetric source vector ``emit``."""
+        s = FEMDomain._sets(mesh, 1, dirichlet_nodes, "all", None, design_elements)
+        return cls(mesh=mesh, neumann_nodes=None, bs=1, k=float(k),
+                   dirichlet_values=float(dirichlet_values),
+                   emit=np.ascontiguousarray(emit, dtype=np.float64), **s)

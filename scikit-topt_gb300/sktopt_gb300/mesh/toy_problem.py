@@ -1,0 +1,66 @@
+"""Benchmark problem set-ups (structured grids, nodal loads).
+
+Cantilever (60x20x20 and 240x80x80 hex workloads): unit hexahedra, all DOFs
+of the nodes on x = 0 clamped, a downward unit load split evenly over the
+nodes of the bottom edge at x = L (x = nx, z = 0) -- or, with ``load_frac``,
+on the single edge node nearest to y = load_frac * ny.  Built through the
+``FEMDomain.from_nodes`` rules (sktopt/mesh/task_common.py:105-270).
+
+Heat box (100x50x50 workload): T = 0 on the nodes of a centred patch of
+``patch`` x ``patch`` elements on z = 0 and a uniform volumetric source.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .grid import create_box_hex, create_box_tet
+from .task import LinearElasticity, LinearHeatConduction
+
+
+def cantilever(nx, ny, nz, E=1.0, nu=0.3, load_frac=None):
+    mesh = create_box_hex(nx, ny, nz)
+    ijk = mesh.node_ijk
+    dn = np.nonzero(ijk[0] == 0)[0]
+    edge = (ijk[0] == nx) & (ijk[2] == 0)
+    if load_frac is None:
+        ln = np.nonzero(edge)[0]
+    else:
+        ln = np.nonzero(edge & (ijk[1] == int(round(load_frac * ny))))[0]
+    f = np.zeros(3 * mesh.nnodes)
+    f[3 * ln + 2] = -1.0 / ln.size
+    tsk = LinearElasticity.from_nodes(mesh, dn, "all", ln, [f], np.arange(mesh.nelements),
+                                      E, nu)
+    return tsk
+
+
+def heat_box(nx, ny, nz, patch=10, source=1.0, k=1.0):
+    from ..fea.composer import source_vector
+    mesh = create_box_hex(nx, ny, nz)
+    ijk = mesh.node_ijk
+    pw = min(patch, nx, ny)
+    x0, y0 = (nx - pw) // 2, (ny - pw) // 2
+    sel = (ijk[2] == 0) & (ijk[0] >= x0) & (ijk[0] <= x0 + pw) & \
+        (ijk[1] >= y0) & (ijk[1] <= y0 + pw)
+    dn = np.nonzero(sel)[0]
+    return LinearHeatConduction.from_nodes(mesh, dn, source_vector(mesh, source),
+                                           np.arange(mesh.nelements), k=k)
+
+
+def multi_load_tet(nx=160, ny=80, nz=40, lx=2.0, ly=1.0, lz=1.0, jitter=0.2, seed=0,
+                   E=1.0, nu=0.3):
+    """Box meshed with jittered P1 tets, bottom face clamped, 4 point-load cases."""
+    mesh = create_box_tet(nx, ny, nz, lx, ly, lz, jitter=jitter, seed=seed)
+    ijk = mesh.node_ijk
+    dn = np.nonzero(ijk[2] == 0)[0]
+    top = np.nonzero(ijk[2] == nz)[0]
+    rng = np.random.default_rng(seed + 1)
+    picks = rng.choice(top, size=2, replace=False)
+    loads, nodes = [], []
+    for node, comp, sign in ((picks[0], 0, 1.0), (picks[0], 1, 1.0), (picks[0], 2, -1.0),
+                             (picks[1], 2, -1.0)):
+        f = np.zeros(3 * mesh.nnodes)
+        f[3 * node + comp] = sign
+        loads.append(f)
+        nodes.append(np.array([node]))
+    return LinearElasticity.from_nodes(mesh, dn, "all", nodes, loads,
+                                       np.arange(mesh.nelements), E, nu)
