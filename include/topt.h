@@ -204,6 +204,19 @@ int topt_design_reduce(topt_filter* f, int32_t op, const double* x, const double
                        const double* w, double c, double rho_min, double rho_max,
                        double* out);
 
+/* Dot product that allocates no device memory, for callers that cannot call
+ * cudaMalloc (a host whose device memory is owned by its own pool, or a loop
+ * that must not stall on the device synchronisation cudaMalloc/cudaFree
+ * imply).  No counterpart in the reference: it is an addition of this
+ * library.  Scratch is a fixed ~32 KB device array per GPU, kept until the
+ * process exits; n is limited to 268,435,456 elements (larger n returns
+ * TOPT_BAD_INPUT).  The first call on a device looks up the array's device
+ * address, so make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (different streams) race.
+ * x, y: dev; out: host. */
+int topt_reduce_dot_noalloc(int64_t n, const double* x, const double* y,
+                            double* out, void* stream);
+
 /* Deterministic reductions (host result). */
 int topt_reduce_max_abs(int64_t n, const double* x, double* out, void* stream);
 int topt_reduce_dot(int64_t n, const double* x, const double* y, double* out,

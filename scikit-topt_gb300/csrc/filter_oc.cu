@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <unordered_map>
 #include <vector>
@@ -640,6 +641,87 @@ int topt_reduce_dot(int64_t n, const double* x, const double* y, double* out, vo
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------------
+// Dot product that allocates nothing.  Some callers cannot call cudaMalloc:
+// a host that gives all device memory to its own pool and forbids stray
+// allocations, or a loop that must not stall on the implicit device
+// synchronisation of cudaMalloc/cudaFree.  For them the reduction scratch
+// (one partial sum per chunk of the input, the last-block arrival counter and
+// the result slot) is a file-scope device array of fixed size, ~32 KB, that
+// every GPU loading the library keeps until the process exits.
+namespace topt {
+
+constexpr int64_t kNoAllocChunk = 65536;   // elements summed by one block
+constexpr int kNoAllocMaxBlocks = 4096;    // partial sums the scratch can hold
+constexpr int64_t kNoAllocMaxN = kNoAllocChunk * kNoAllocMaxBlocks;  // 268,435,456
+
+struct NoAllocScratch {
+  double partials[kNoAllocMaxBlocks];
+  double result;
+  unsigned counter;
+};
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Block b sums x[i] * y[i] over its chunk [b*chunk, (b+1)*chunk); the last
+// block to finish adds the partials in block order (deterministic).
+__global__ void k_dot_chunked(int64_t n, const double* __restrict__ x,
+                              const double* __restrict__ y, NoAllocScratch* s) {
+  TOPT_KERNEL_COUNT();
+  const int64_t b0 = (int64_t)blockIdx.x * kNoAllocChunk;
+  const int64_t b1 = b0 + kNoAllocChunk < n ? b0 + kNoAllocChunk : n;
+  double acc[1] = {0.0};
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc[0] += x[i] * y[i];
+  __shared__ double sh[32];
+  block_sum<double, 1>(acc, sh);
+  grid_finish<double, 1>(acc, s->partials, &s->counter, &s->result);
+}
+
+// Device address of the scratch array, looked up once per device (host code
+// only holds a host-side stand-in for the symbol; kernels need this address).
+static int noalloc_scratch_address(NoAllocScratch** out) {
+  static std::mutex mu;
+  static NoAllocScratch* addr[64] = {};
+  int dev = 0;
+  TOPT_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(TOPT_BAD_INPUT, "reduce_dot_noalloc: device id >= 64");
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void* p = nullptr;
+    TOPT_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    addr[dev] = static_cast<NoAllocScratch*>(p);
+  }
+  *out = addr[dev];
+  return TOPT_OK;
+}
+
+}  // namespace topt
+
+extern "C" int topt_reduce_dot_noalloc(int64_t n, const double* x, const double* y,
+                                       double* out, void* stream) {
+  using namespace topt;
+  if (!out || n < 0 || (n > 0 && (!x || !y)))
+    return fail(TOPT_BAD_INPUT, "reduce_dot_noalloc: bad argument");
+  if (n > kNoAllocMaxN)
+    return fail(TOPT_BAD_INPUT, "reduce_dot_noalloc: n exceeds the maximum of 268435456 "
+                                "elements that the fixed scratch supports");
+  if (n == 0) {
+    *out = 0.0;
+    return TOPT_OK;
+  }
+  NoAllocScratch* s = nullptr;
+  int rc = noalloc_scratch_address(&s);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  // the arrival counter must start at zero whatever the previous call left
+  TOPT_CUDA(cudaMemsetAsync(&s->counter, 0, sizeof(unsigned), st));
+  const int blocks = (int)((n + kNoAllocChunk - 1) / kNoAllocChunk);
+  k_dot_chunked<<<blocks, kFB, 0, st>>>(n, x, y, s);
+  TOPT_CHECK_LAUNCH("k_dot_chunked");
+  TOPT_CUDA(cudaMemcpyAsync(out, &s->result, sizeof(double), cudaMemcpyDeviceToHost, st));
+  TOPT_CUDA(cudaStreamSynchronize(st));
+  return TOPT_OK;
+}
 
 namespace topt {
 int launches_filter(unsigned long long* out) {

@@ -106,6 +106,7 @@ SIGNATURES = {
     "topt_design_reduce": (C.c_int, [_P, _I32, _P, _P, _P, _D, _D, _D, C.POINTER(_D)]),
     "topt_reduce_max_abs": (C.c_int, [_I64, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
+    "topt_reduce_dot_noalloc": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
 }
 
 _lib = None
