@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
+    ap.add_argument("--probe", choices=["spmv"], default=None,
+                    help="profiling target instead of the benchmark")
     return ap.parse_args()
 
 
@@ -177,10 +179,14 @@ def spmv_roofline(opt, peak_gbs):
     nb = eng.nnzb
     bytes_alg = nb * (9 * 4 + 4) + 4 * (eng.mesh.nnodes + 1) + 2 * 4 * eng.n_dof
     achieved = bytes_alg / t / 1e9
+    # DRAM traffic per launch from the ncu capture of the same kernel on the
+    # 120x40x40 cantilever (profiles/sell_spmv_fp32_120x40x40.md): 222.19 MB
+    # for 5,285,401 blocks = 42.04 B per block, scaled to this launch's blocks.
+    traffic = 42.04 * nb
     return {"kernel": "k_sell_spmv<float,3,1> (level-0 FP32 SpMV)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
             "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_alg),
-            "launch_us": round(t * 1e6, 1)}
+            "launch_us": round(t * 1e6, 1), "traffic": int(traffic)}
 
 
 def run_gpu(args):
@@ -268,7 +274,7 @@ def run_gpu(args):
                    "parallelism": f"replicas x{world}",
                    "l2": "working set (>4 GB per step) exceeds the 129 MB L2"},
         "e2e": e2e, "gpu_launches": int(launches),
-        "roofline": dict(roof, traffic=None, peak_kind=peak_kind),
+        "roofline": dict(roof, peak_kind=peak_kind),
         "fp64_path": fp64,
         "compliance_rel_err_same_density": same_density_err,
         "mixed_solver_iters": mixed_stats[-args.steps:],
@@ -362,8 +368,39 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def probe_spmv(size):
+    """Profiling target: assemble the mixed engine for a cantilever of `size`
+    and run the level-0 SpMV twice in FP32 (NVTX range "spmv32") and twice in
+    FP64 (range "spmv64")."""
+    import numpy as np
+    import torch
+    from sktopt_gb300.fea import composer
+    from sktopt_gb300.fea.engine import FemEngine
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", 0)
+    tsk = toy_problem.cantilever(*size)
+    Ke, _, _ = composer.element_matrices(tsk.mesh, 0.3)
+    eng = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True)
+    eng.update(torch.full((tsk.mesh.nelements,), 0.5, dtype=torch.float64, device=dev),
+               1.0, 1e-9, 3.0)
+    x32 = torch.rand((eng.n_dof, 1), dtype=torch.float32, device=dev)
+    x64 = x32.double()
+    torch.cuda.synchronize()
+    for name, x, dt in (("spmv32", x32, torch.float32), ("spmv64", x64, torch.float64)):
+        torch.cuda.nvtx.range_push(name)
+        for _ in range(2):
+            eng.spmv(x, dt)
+        torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    print(json.dumps({"probe": "spmv", "size": list(size), "nnzb": eng.nnzb,
+                      "n_dof": eng.n_dof}))
+
+
 def main():
     args = parse()
+    if args.probe == "spmv":
+        probe_spmv(tuple(args.size))
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
