@@ -179,9 +179,10 @@ def spmv_roofline(opt, peak_gbs):
     nb = eng.nnzb
     bytes_alg = nb * (9 * 4 + 4) + 4 * (eng.mesh.nnodes + 1) + 2 * 4 * eng.n_dof
     achieved = bytes_alg / t / 1e9
-    # DRAM traffic per launch from the ncu capture of the same kernel on the
-    # 120x40x40 cantilever (profiles/sell_spmv_fp32_120x40x40.md): 222.19 MB
-    # for 5,285,401 blocks = 42.04 B per block, scaled to this launch's blocks.
+    # DRAM traffic per launch: an ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum) of this kernel on the 120x40x40 cantilever read
+    # and wrote 222.19 MB for 5,285,401 blocks = 42.04 B per block; scaled here
+    # to this launch's block count.
     traffic = 42.04 * nb
     return {"kernel": "k_sell_spmv<float,3,1> (level-0 FP32 SpMV)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",

@@ -204,6 +204,61 @@ int topt_design_reduce(topt_filter* f, int32_t op, const double* x, const double
                        const double* w, double c, double rho_min, double rho_max,
                        double* out);
 
+/* Identity filter (W = I on the design elements): a design-set handle for the
+ * stepwise bisection and the design operations below when the density filter
+ * is not a fixed matrix (HelmholtzFilterNodal, helmholtz_filter_nodal.py). */
+int topt_filter_identity_create(int64_t n_elem, const uint8_t* design_mask,
+                                topt_filter** out);
+
+/* The OC bisection one step at a time (oc.py:16-95) for any filter:
+ * topt_oc_begin gathers the current design densities and resets the
+ * multiplier bracket; each step, topt_oc_candidate writes the candidate's
+ * design entries into `cand` (full length; the caller keeps the non-design
+ * entries), the caller filters cand, and topt_oc_volume projects the
+ * filtered field, sums the design volume and advances the bracket (host
+ * outputs; done = 1 once a stopping rule of oc.py:81-86 fired);
+ * topt_oc_finish writes the accepted candidate into rho. */
+int topt_oc_begin(topt_filter* f, const double* rho, const topt_oc_params* prm);
+int topt_oc_candidate(topt_filter* f, const double* dc, double dc_scale,
+                      const topt_oc_params* prm, double* cand, double* scaling);
+int topt_oc_volume(topt_filter* f, const double* filtered, const double* vol,
+                   double vol_sum, const topt_oc_params* prm, int32_t* done,
+                   double* lmid, double* vol_error, int32_t* steps);
+int topt_oc_finish(topt_filter* f, double* rho);
+
+/* out[i] = x[d_i] + c y[d_i] over the design elements d_i (y may be NULL);
+ * the LogMOC Lagrangian gradient dL = dC + coeff dV_chain (logmoc.py:
+ * 204-215). */
+int topt_design_gather_axpy(topt_filter* f, const double* x, const double* y,
+                            double c, double* out);
+/* sum_i x[d_i] w[i] (host result; the design volume of logmoc.py:160-163). */
+int topt_design_wsum(topt_filter* f, const double* x, const double* w,
+                     double* out);
+/* max |c w[i]| over interior design elements (logmoc.py:227-236). */
+int topt_design_kkt(topt_filter* f, const double* rho, const double* w, double c,
+                    double rho_min, double rho_max, double* out);
+/* lagrangian_log_update (logmoc.py:36-66) with dL = dl * inv_scale on the
+ * design elements of rho (in place); scaling (design order) may be NULL. */
+int topt_logmoc_update(topt_filter* f, const double* dl, double inv_scale, double* rho,
+                       double eta, double move_limit, double rho_min, double rho_max,
+                       double lagrangian_clip, double* scaling);
+/* numpy.percentile(|x[idx]|, q) with the default 'linear' method (radix
+ * select, deterministic); idx may be NULL (all of x).  Used for the OC
+ * percentile scaling (oc.py:186-189) and the LogMOC scale (logmoc.py:217-225). */
+int topt_percentile_abs(int64_t n, const int32_t* idx, const double* x, double q,
+                        double* out, void* stream);
+
+/* Helmholtz nodal filter transfers (helmholtz_filter_nodal.py:26-56):
+ * volume-weighted element -> node average over the node's elements (CSR
+ * node_ptr/node_elems), non-design elements contributing fixed_value
+ * (design may be NULL = all design); and node -> element mean, optionally
+ * clamped to <= 0 (the gradient's clamp, helmholtz_filter_nodal.py:232). */
+int topt_elem_to_node(int64_t n_nodes, const int32_t* node_ptr, const int32_t* node_elems,
+                      const double* vol, const double* x, const uint8_t* design,
+                      double fixed_value, double* out, void* stream);
+int topt_node_to_elem(int64_t n_elem, int32_t nloc, const int32_t* t, const double* x_node,
+                      int32_t clamp_nonpositive, double* out, void* stream);
+
 /* Dot product that allocates no device memory, for callers that cannot call
  * cudaMalloc (a host whose device memory is owned by its own pool, or a loop
  * that must not stall on the device synchronisation cudaMalloc/cudaFree

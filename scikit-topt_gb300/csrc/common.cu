@@ -42,6 +42,9 @@ extern "C" int topt_launch_count(uint64_t* out) {
   if (rc) return rc;
   rc = topt::launches_filter(&b);
   if (rc) return rc;
-  *out = (uint64_t)(a + b);
+  unsigned long long c = 0;
+  rc = topt::launches_design(&c);
+  if (rc) return rc;
+  *out = (uint64_t)(a + b + c);
   return TOPT_OK;
 }

@@ -5,7 +5,7 @@
 // functions (sktopt/core/projection.py:27-118), bisection_with_physical_volume
 // (sktopt/core/optimizers/oc.py:16-95) and lagrangian_log_update
 // (sktopt/core/optimizers/logmoc.py:36-66).
-#include "cuda_common.cuh"
+#include "filter_internal.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -14,31 +14,6 @@
 #include <new>
 #include <unordered_map>
 #include <vector>
-
-namespace topt {
-
-static const int kFB = 256;
-
-struct OcState {
-  double l1, l2, lmid, vol_error;
-  int it, done, steps, pad;
-};
-
-}  // namespace topt
-
-struct topt_filter {
-  int64_t n_elem = 0, n_design = 0, nnz = 0;
-  cudaStream_t stream = nullptr;
-  int sm = 152;
-  std::vector<int32_t> h_rowptr, h_colind;   // design-local columns
-  std::vector<double> h_vals;
-  topt::DevBuf design, nondesign;            // element ids
-  topt::DevBuf rowptr, colfull, vals;        // W with full-element columns
-  topt::DevBuf t_rowptr, t_colfull, t_vals;  // W^T
-  int64_t n_nondesign = 0;
-  // OC work
-  topt::DevBuf cand, state, partials, counter, rho_e, rho_new;
-};
 
 namespace topt {
 

@@ -104,6 +104,19 @@ SIGNATURES = {
     "topt_oc_bisect": (C.c_int, [_P, _P, _D, _P, _P, _D, C.POINTER(OcParams), _P,
                                  C.POINTER(_D), C.POINTER(_D), C.POINTER(_I32)]),
     "topt_design_reduce": (C.c_int, [_P, _I32, _P, _P, _P, _D, _D, _D, C.POINTER(_D)]),
+    "topt_filter_identity_create": (C.c_int, [_I64, _P, C.POINTER(_P)]),
+    "topt_oc_begin": (C.c_int, [_P, _P, C.POINTER(OcParams)]),
+    "topt_oc_candidate": (C.c_int, [_P, _P, _D, C.POINTER(OcParams), _P, _P]),
+    "topt_oc_volume": (C.c_int, [_P, _P, _P, _D, C.POINTER(OcParams), C.POINTER(_I32),
+                                 C.POINTER(_D), C.POINTER(_D), C.POINTER(_I32)]),
+    "topt_oc_finish": (C.c_int, [_P, _P]),
+    "topt_design_gather_axpy": (C.c_int, [_P, _P, _P, _D, _P]),
+    "topt_design_wsum": (C.c_int, [_P, _P, _P, C.POINTER(_D)]),
+    "topt_design_kkt": (C.c_int, [_P, _P, _P, _D, _D, _D, C.POINTER(_D)]),
+    "topt_logmoc_update": (C.c_int, [_P, _P, _D, _P, _D, _D, _D, _D, _D, _P]),
+    "topt_percentile_abs": (C.c_int, [_I64, _P, _P, _D, C.POINTER(_D), _P]),
+    "topt_elem_to_node": (C.c_int, [_I64, _P, _P, _P, _P, _P, _D, _P, _P]),
+    "topt_node_to_elem": (C.c_int, [_I64, _I32, _P, _P, _I32, _P, _P]),
     "topt_reduce_max_abs": (C.c_int, [_I64, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot_noalloc": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),

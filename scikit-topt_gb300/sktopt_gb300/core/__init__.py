@@ -1,5 +1,5 @@
 from .optimizers import (DensityMethod, DensityMethodConfig, DensityMethod_OC_Config,
-                         OC_Config, OC_Optimizer)
+                         LogMOC_Config, LogMOC_Optimizer, OC_Config, OC_Optimizer)
 
 __all__ = ["DensityMethod", "DensityMethodConfig", "DensityMethod_OC_Config", "OC_Config",
-           "OC_Optimizer"]
+           "OC_Optimizer", "LogMOC_Config", "LogMOC_Optimizer"]

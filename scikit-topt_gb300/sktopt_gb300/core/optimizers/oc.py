@@ -57,21 +57,17 @@ class OC_Optimizer(DensityMethod):
                          scaling_max=cfg.scaling_rate_max, vol_tol=1e-4,
                          l1=cfg.lambda_lower, l2=cfg.lambda_upper, tolerance=1e-5,
                          max_iter=1000)
-        lmid, verr, steps = C.c_double(), C.c_double(), C.c_int32()
-        flt._bind()
-        N.check(N.load().topt_oc_bisect(
-            flt.h, C.c_void_p(st.dC_drho_full.data_ptr()), float(self.running_scale),
-            C.c_void_p(st.rho.data_ptr()), C.c_void_p(self._vol_design.data_ptr()),
-            self._vol_design_sum, C.byref(prm), C.c_void_p(st.scaling_rate.data_ptr()),
-            C.byref(lmid), C.byref(verr), C.byref(steps)))
+        lmid, verr, steps = flt.oc_bisect(st.dC_drho_full, self.running_scale, st.rho,
+                                          self._vol_design, self._vol_design_sum, prm,
+                                          st.scaling_rate)
         # KKT over interior design elements: |dC_raw + lmid * scale * dV| (oc.py:230-240)
         self.kkt_residual = flt.design_reduce(2, st.dC_drho_full, st.rho,
                                               w=self._dV_drho_design,
-                                              c=lmid.value * self.running_scale,
+                                              c=lmid * self.running_scale,
                                               rho_min=cfg.rho_min, rho_max=cfg.rho_max)
-        st.vol_error = verr.value
+        st.vol_error = verr
         st.kkt_residual = self.kkt_residual
-        self.last_bisection_steps = steps.value
-        self.recorder.feed_data("lmid", lmid.value)
-        self.recorder.feed_data("vol_error", verr.value)
+        self.last_bisection_steps = steps
+        self.recorder.feed_data("lmid", lmid)
+        self.recorder.feed_data("vol_error", verr)
         self.recorder.feed_data("kkt_residual", self.kkt_residual)

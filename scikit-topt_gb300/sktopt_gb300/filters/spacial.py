@@ -15,20 +15,24 @@ import numpy as np
 import torch
 
 from .. import _native as N
-from .._device import as_device, default_device, stream_handle
+from .._device import as_device, default_device
 from ..mesh.grid import element_centers
-from .base import BaseFilter
+from .base import BaseFilter, DesignOps
 
 
-class SpacialFilter(BaseFilter):
+class SpacialFilter(DesignOps, BaseFilter):
+    fused_bisection = True
+
     def __init__(self, mesh, elements_volume, radius, design_mask=None, device=None):
-        super().__init__(mesh, elements_volume, radius, design_mask)
+        BaseFilter.__init__(self, mesh, elements_volume, radius, design_mask)
         self.lib = N.load()
         self.device = device or default_device()
         self.element_centers = np.ascontiguousarray(element_centers(mesh))
         n = mesh.nelements
         self._mask = np.ones(n, np.uint8) if design_mask is None else \
             np.ascontiguousarray(design_mask, dtype=np.uint8)
+        self._design_idx = torch.from_numpy(
+            np.nonzero(self._mask)[0].astype(np.int32)).to(self.device)
         self.h = None
         self._build(radius)
 
@@ -64,9 +68,6 @@ class SpacialFilter(BaseFilter):
         if radius != self.radius:
             self._build(radius)
 
-    def _bind(self):
-        N.check(self.lib.topt_filter_set_stream(self.h, C.c_void_p(stream_handle())))
-
     def forward_device(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         self._bind()
         y = torch.empty_like(x) if out is None else out
@@ -92,17 +93,6 @@ class SpacialFilter(BaseFilter):
         x = as_device(v, device=self.device)
         y = self.gradient_device(x)
         return y if isinstance(v, torch.Tensor) else y.cpu().numpy()
-
-    def design_reduce(self, op, x, y=None, w=None, c=0.0, rho_min=0.0, rho_max=1.0) -> float:
-        """Max-type reductions over the design elements (topt_design_reduce)."""
-        self._bind()
-        out = C.c_double()
-        N.check(self.lib.topt_design_reduce(
-            self.h, int(op), C.c_void_p(x.data_ptr()),
-            C.c_void_p(y.data_ptr()) if y is not None else None,
-            C.c_void_p(w.data_ptr()) if w is not None else None, float(c), float(rho_min),
-            float(rho_max), C.byref(out)))
-        return out.value
 
     def export_matrix(self):
         """W as (indptr, indices, data) over design-element positions."""
