@@ -157,37 +157,49 @@ def timed_run(opt, warmup, steps, sampler=None):
     return ms, wall, l1 - l0, clocks
 
 
-def spmv_roofline(opt, peak_gbs):
-    """Level-0 FP32 SpMV (the dominant kernel of the mixed solve) timed with CUDA
-    events on the launching stream; algorithmic bytes per launch:
-    nnzb*(9*4 + 4) + 4*(n_nodes+1) + 2*4*n_dof."""
+def _event_time(fn, n=20):
     import torch
-    eng = opt.fem.engine
-    x = torch.rand((eng.n_dof, 1), dtype=torch.float32, device=eng.device)
     for _ in range(3):
-        eng.spmv(x, torch.float32)
+        fn()
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    n = 20
     torch.cuda.synchronize()
     e0.record(s)
     for _ in range(n):
-        eng.spmv(x, torch.float32)
+        fn()
     e1.record(s)
     torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / n * 1e-3
+    return e0.elapsed_time(e1) / n * 1e-3
+
+
+def spmv_roofline(opt, peak_gbs):
+    """The dominant kernel of the mixed solve: the FP64 SELL SpMV of the outer
+    flexible CG (one per iteration), timed with CUDA events on the launching
+    stream.  Algorithmic bytes per launch (3x3 BSR, FP64 values, int32 block
+    columns): nnzb*(9*8 + 4) + 4*(n_nodes+1) + 2*8*n_dof.  The FP32 fine-level
+    operator of the inner V-cycle is matrix-free (compute-bound) and reported
+    separately."""
+    import torch
+    eng = opt.fem.engine
+    x64 = torch.rand((eng.n_dof, 1), dtype=torch.float64, device=eng.device)
+    x32 = x64.float()
+    t = _event_time(lambda: eng.spmv(x64))
+    t32 = _event_time(lambda: eng.spmv(x32, torch.float32))
     nb = eng.nnzb
-    bytes_alg = nb * (9 * 4 + 4) + 4 * (eng.mesh.nnodes + 1) + 2 * 4 * eng.n_dof
+    bytes_alg = nb * (9 * 8 + 4) + 4 * (eng.mesh.nnodes + 1) + 2 * 8 * eng.n_dof
     achieved = bytes_alg / t / 1e9
     # DRAM traffic per launch: an ncu capture (dram__bytes_read.sum +
     # dram__bytes_write.sum) of this kernel on the 120x40x40 cantilever read
-    # and wrote 222.19 MB for 5,285,401 blocks = 42.04 B per block; scaled here
+    # and wrote 425.16 MB for 5,285,401 blocks = 80.44 B per block; scaled here
     # to this launch's block count.
-    traffic = 42.04 * nb
-    return {"kernel": "k_sell_spmv<float,3,1> (level-0 FP32 SpMV)", "bound": "hbm",
-            "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+    traffic = 80.44 * nb
+    mf_flops = 2 * 576 * eng.mesh.nnodes
+    return {"kernel": "k_sell_spmv<double,3,1> (fine-level FP64 SpMV, outer FCG)",
+            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
             "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_alg),
-            "launch_us": round(t * 1e6, 1), "traffic": int(traffic)}
+            "launch_us": round(t * 1e6, 1), "traffic": int(traffic),
+            "fp32_matrix_free_us": round(t32 * 1e6, 1),
+            "fp32_matrix_free_tflops": round(mf_flops / t32 / 1e12, 2)}
 
 
 def run_gpu(args):

@@ -85,6 +85,9 @@ typedef struct topt_fem_desc {
   int32_t mixed;              /* keep an FP32 operator + hierarchy as well   */
   int32_t mg_levels;          /* max multigrid levels (1 = no coarsening)    */
   int32_t mg_coarse_max;      /* dense direct solve at <= this many DOFs     */
+  int32_t mf_level0;          /* mixed, uniform hex elasticity: apply the FP32
+                                 fine-level operator matrix-free from the
+                                 shared element matrix (no FP32 assembly)    */
 } topt_fem_desc;
 
 int topt_fem_create(const topt_fem_desc* d, topt_fem** out);

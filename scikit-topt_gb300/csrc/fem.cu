@@ -32,7 +32,7 @@ struct LevelStruct {
   // cell -> element lists (level 0 only, when elements are not the cells)
   DevBuf cell_ptr, cell_elems;
   // transfer tables to the next coarser level (per axis)
-  DevBuf cmx, cmy, cmz, c0x, c0y, c0z, w1x, w1y, w1z;
+  DevBuf cmx, cmy, cmz, c0x, c0y, c0z, w1x, w1y, w1z, r0x, r0y, r0z, rwx, rwy, rwz;
   GridT grid{};
   // shared-matrix Galerkin fast path (level 0 -> 1 of uniform hex meshes)
   DevBuf gal_M64, gal_M32, gal_masked, gal_list;
@@ -96,6 +96,10 @@ struct topt_fem {
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   bool assembled = false;
+  // matrix-free FP32 level-0 operator (uniform hex grid, shared unit matrix)
+  bool mf = false;
+  topt::MfGrid mfg{};
+  topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
 };
 
 namespace topt {
@@ -239,6 +243,37 @@ static int make_transfer(LevelStruct& F, const LevelStruct& Cs, cudaStream_t s) 
   g.cmx = F.cmx.as<int32_t>(); g.cmy = F.cmy.as<int32_t>(); g.cmz = F.cmz.as<int32_t>();
   g.c0x = F.c0x.as<int32_t>(); g.c0y = F.c0y.as<int32_t>(); g.c0z = F.c0z.as<int32_t>();
   g.w1x = F.w1x.as<double>(); g.w1y = F.w1y.as<double>(); g.w1z = F.w1z.as<double>();
+  // restriction tables: coarse node i gathers fine nodes r0[i] + k, k < 3,
+  // with the hat weights of its interpolation (P^T row)
+  std::vector<int32_t> r0[3];
+  std::vector<float> rw[3];
+  for (int d = 0; d < 3; ++d) {
+    const std::vector<int32_t>& c = cm[d];
+    const int nc = (int)c.size() - 1;
+    r0[d].resize(nc + 1);
+    rw[d].assign(3 * (nc + 1), 0.0f);
+    for (int i = 0; i <= nc; ++i) {
+      const int f0 = i > 0 ? c[i - 1] + 1 : 0;
+      const int f1 = i < nc ? c[i + 1] - 1 : nf[d];
+      r0[d][i] = f0;
+      for (int f = f0; f <= f1 && f - f0 < 3; ++f) {
+        double w;
+        if (f == c[i]) w = 1.0;
+        else if (f < c[i]) w = (double)(f - c[i - 1]) / (double)(c[i] - c[i - 1]);
+        else w = (double)(c[i + 1] - f) / (double)(c[i + 1] - c[i]);
+        rw[d][3 * i + (f - f0)] = (float)w;
+      }
+    }
+  }
+  if ((rc = upload(F.r0x, r0[0].data(), r0[0].size(), s))) return rc;
+  if ((rc = upload(F.r0y, r0[1].data(), r0[1].size(), s))) return rc;
+  if ((rc = upload(F.r0z, r0[2].data(), r0[2].size(), s))) return rc;
+  if ((rc = upload(F.rwx, rw[0].data(), rw[0].size(), s))) return rc;
+  if ((rc = upload(F.rwy, rw[1].data(), rw[1].size(), s))) return rc;
+  if ((rc = upload(F.rwz, rw[2].data(), rw[2].size(), s))) return rc;
+  TOPT_CUDA(cudaStreamSynchronize(s));
+  g.r0x = F.r0x.as<int32_t>(); g.r0y = F.r0y.as<int32_t>(); g.r0z = F.r0z.as<int32_t>();
+  g.rwx = F.rwx.as<float>(); g.rwy = F.rwy.as<float>(); g.rwz = F.rwz.as<float>();
   return TOPT_OK;
 }
 
@@ -267,6 +302,14 @@ static int assemble(topt_fem* h, const LevelStruct& L, int bs, int nloc, const T
 template <typename T, int BS, int L, int MODE, bool DOT>
 static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const T* x,
                        const T* b, T* y, int red_slot) {
+  if (Ls.n_nodes <= 65536) {   // coarse levels: one warp per row
+    const int g = gridsize(h, Ls.n_nodes * 32);
+    k_sell_spmv_warp<T, BS, L, MODE, DOT><<<g, kBlock, 0, h->stream>>>(
+        Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
+        h->red.res(red_slot));
+    TOPT_CHECK_LAUNCH("k_sell_spmv_warp");
+    return TOPT_OK;
+  }
   const int g = gridsize(h, Ls.n_nodes);
   k_sell_spmv<T, BS, L, MODE, DOT><<<g, kBlock, 0, h->stream>>>(
       Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
@@ -276,9 +319,51 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 }
 
 // MODE 0 y=Ax, 1 y=b-Ax, 2 y-=Ax; dot -> red slot
+// The single-load matrix-free kernel reads K0 from constant memory; the
+// constant bank is per process, so it is (re)loaded on the handle's stream
+// whenever another handle's K0 was loaded last.
+static const void* g_k0_owner = nullptr;
+
+template <int L, int MODE, bool DOT>
+static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  if (L == 1) {
+    if (g_k0_owner != h->ke32.p) {
+      TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->ke32.p, 576 * sizeof(float), 0,
+                                        cudaMemcpyDeviceToDevice, h->stream));
+      g_k0_owner = h->ke32.p;
+    }
+    k_mf_apply1<MODE, DOT><<<gridsize(h, h->n_nodes, 128), 128, 0, h->stream>>>(
+        h->mfg, h->coef32.as<float>(), h->nmask.as<uint8_t>(), x, b, y,
+        h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
+    TOPT_CHECK_LAUNCH("k_mf_apply1");
+    return TOPT_OK;
+  }
+  k_mf_apply<float, L, MODE, DOT><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
+      h->mfg, h->ke32.as<float>(), h->coef32.as<float>(), h->mask.as<uint8_t>(), x, b, y,
+      h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
+  TOPT_CHECK_LAUNCH("k_mf_apply");
+  return TOPT_OK;
+}
+
+static int mf_spmv(topt_fem* h, int L, int mode, bool dot, const float* x, const float* b,
+                   float* y, int slot) {
+#define TOPT_MF_CASE(L_)                                                          \
+  if (L == L_) {                                                                  \
+    if (mode == 0 && !dot) return launch_mf<L_, 0, false>(h, x, b, y, slot);      \
+    if (mode == 0 && dot) return launch_mf<L_, 0, true>(h, x, b, y, slot);        \
+    if (mode == 1) return launch_mf<L_, 1, false>(h, x, b, y, slot);              \
+    if (mode == 2) return launch_mf<L_, 2, false>(h, x, b, y, slot);              \
+  }
+  TOPT_MF_CASE(1) TOPT_MF_CASE(2) TOPT_MF_CASE(3) TOPT_MF_CASE(4)
+#undef TOPT_MF_CASE
+  return fail(TOPT_BAD_INPUT, "mf_spmv: unsupported nrhs");
+}
+
 template <typename T>
 static int spmv(topt_fem* h, const LevelStruct& Ls, int bs, int L, int mode, bool dot,
                 const T* vals, const T* x, const T* b, T* y, int slot = 0) {
+  if (std::is_same<T, float>::value && h->mf && &Ls == &h->ls[0])
+    return mf_spmv(h, L, mode, dot, (const float*)x, (const float*)b, (float*)y, slot);
 #define TOPT_SPMV_CASE(BS_, L_)                                                        \
   if (bs == BS_ && L == L_) {                                                          \
     if (mode == 0 && !dot) return launch_spmv<T, BS_, L_, 0, false>(h, Ls, vals, x, b, y, slot); \
@@ -347,7 +432,8 @@ static int alloc_level_num(topt_fem* h, LevelNum<T>& N, const LevelStruct& L, in
   int rc;
   const int64_t nd = L.n_nodes * bs;
   if (li > 0 && (rc = N.ke.alloc(sizeof(T) * L.n_elem * 64 * bs * bs))) return rc;
-  if ((rc = N.vals.alloc(sizeof(T) * L.npos * bs * bs))) return rc;
+  const bool mf0 = std::is_same<T, float>::value && h->mf && li == 0;
+  if (!mf0 && (rc = N.vals.alloc(sizeof(T) * L.npos * bs * bs))) return rc;
   if ((rc = N.dinv.alloc(sizeof(T) * L.n_nodes * bs * bs))) return rc;
   for (DevBuf* b : {&N.b, &N.x, &N.r, &N.d, &N.q})
     if ((rc = b->alloc(sizeof(T) * nd * 4))) return rc;
@@ -571,13 +657,21 @@ static int refresh(topt_fem* h, Hier<T>& H) {
   }
   const int bs = h->bs;
   const int64_t stride0 = h->n_ke == 1 ? 0 : (int64_t)(bs * h->nloc) * (bs * h->nloc);
-  // level 0 operator
-  if ((rc = assemble<T>(h, h->ls[0], bs, h->nloc, level0_ke<T>(h), stride0, level0_coef<T>(h),
-                        h->mask.as<uint8_t>(), H.lv[0].vals.template as<T>())))
-    return rc;
-  if ((rc = block_inv<T>(h, h->ls[0], H.lv[0].vals.template as<T>(),
-                         H.lv[0].dinv.template as<T>(), false)))
-    return rc;
+  // level 0 operator (FP32 of a uniform hex grid: matrix-free, diagonal only)
+  if (std::is_same<T, float>::value && h->mf) {
+    k_mf_diag_inv<float><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
+        h->mfg, h->ke32.as<float>(), h->coef32.as<float>(), h->mask.as<uint8_t>(),
+        (float*)H.lv[0].dinv.p);
+    TOPT_CHECK_LAUNCH("k_mf_diag_inv");
+  } else {
+    if ((rc = assemble<T>(h, h->ls[0], bs, h->nloc, level0_ke<T>(h), stride0,
+                          level0_coef<T>(h), h->mask.as<uint8_t>(),
+                          H.lv[0].vals.template as<T>())))
+      return rc;
+    if ((rc = block_inv<T>(h, h->ls[0], H.lv[0].vals.template as<T>(),
+                           H.lv[0].dinv.template as<T>(), false)))
+      return rc;
+  }
   DevBuf scratch;
   for (int li = 0; li < nlev; ++li) {
     LevelStruct& L = h->ls[li];
@@ -1035,6 +1129,18 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
     }
     if (h->ls.size() > 1 && d->n_ke == 1 && d->nloc == 8 && !d->cell_of_elem) {
       if ((rc = setup_shared_galerkin(h.get(), d->ke, d->dirichlet))) return rc;
+    }
+    // matrix-free FP32 level 0 on uniform hex grids (elasticity)
+    if (d->n_ke == 1 && d->nloc == 8 && d->bs == 3 && !d->cell_of_elem && d->mixed &&
+        d->mf_level0) {
+      h->mf = true;
+      h->mfg.nx = nx; h->mfg.ny = ny; h->mfg.nz = nz;
+      std::vector<uint8_t> nm(d->n_nodes);
+      for (int64_t n = 0; n < d->n_nodes; ++n)
+        nm[n] = (uint8_t)((d->dirichlet[3 * n] ? 1 : 0) | (d->dirichlet[3 * n + 1] ? 2 : 0) |
+                          (d->dirichlet[3 * n + 2] ? 4 : 0));
+      if ((rc = upload(h->nmask, nm.data(), nm.size(), s))) return rc;
+      TOPT_CUDA(cudaStreamSynchronize(s));
     }
     if (h->ls.size() > 1) {
       LevelStruct& B = h->ls.back();

@@ -43,6 +43,10 @@ struct SellT {
   const int32_t* diag;          // nrows, position of the diagonal block
 };
 
+// local node offsets of a hex cell (MeshHex order)
+__constant__ int c_hex_off[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1},
+                                    {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 1}};
+
 template <int BS>
 __device__ __forceinline__ int64_t vidx(int64_t p, int v) {
   return ((p >> 5) * (BS * BS) + v) * 32 + (p & 31);
@@ -201,6 +205,278 @@ k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
         else out = y[idx] - acc[i];
         y[idx] = out;
         if (DOT) dacc[i % L] += (double)x[idx] * (double)out;
+      }
+    }
+  }
+  if (DOT) {
+    __shared__ double sh[32 * L];
+    block_sum<double, L>(dacc, sh);
+    grid_finish<double, L>(dacc, partials, counter, dot_out);
+  }
+}
+
+// --------------------------------------------------------------------------
+// Matrix-free operator of a uniform hex grid (one shared unit matrix K0):
+// y_a = sum over the <= 8 cells c around node a of coef_c * K0[la, :] x_c,
+// with la the node's local index in c.  One thread per node, K0 in shared
+// memory (every lane of a warp reads the same K0 row: broadcast), the x of
+// the 27 neighbouring nodes from L1.  Fixed DOFs act as identity rows and
+// zero columns (skfem.enforce).  Compute-bound FP32 instead of streaming the
+// assembled blocks.  MODE and DOT as k_sell_spmv.
+struct MfGrid {
+  int nx, ny, nz;  // cells
+};
+
+template <typename T, int L, int MODE, bool DOT>
+__global__ void __launch_bounds__(256)
+k_mf_apply(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
+           const uint8_t* __restrict__ mask, const T* __restrict__ x,
+           const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
+           double* dot_out) {
+  TOPT_KERNEL_COUNT();
+  __shared__ T Ks[24 * 24];
+  for (int i = threadIdx.x; i < 576; i += blockDim.x) Ks[i] = K0[i];
+  __syncthreads();
+  const int ny1 = g.ny + 1, nx1 = g.nx + 1;
+  const int64_t nn = (int64_t)nx1 * ny1 * (g.nz + 1);
+  double dacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nn;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const int ai = (int)a;  // node counts fit 32 bits: cheap index math
+    const int iy = ai % ny1;
+    const int ix = (ai / ny1) % nx1;
+    const int iz = ai / (ny1 * nx1);
+    T acc[3 * L];
+#pragma unroll
+    for (int q = 0; q < 3 * L; ++q) acc[q] = T(0);
+#pragma unroll
+    for (int la = 0; la < 8; ++la) {
+      // cell whose local node la is this node
+      const int cx = ix - c_hex_off[la][0], cy = iy - c_hex_off[la][1],
+                cz = iz - c_hex_off[la][2];
+      if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
+      const T s = coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
+      T part[3 * L];
+#pragma unroll
+      for (int q = 0; q < 3 * L; ++q) part[q] = T(0);
+#pragma unroll
+      for (int lb = 0; lb < 8; ++lb) {
+        const int64_t nb = (cy + c_hex_off[lb][1]) +
+                           (int64_t)ny1 * ((cx + c_hex_off[lb][0]) +
+                                           (int64_t)nx1 * (cz + c_hex_off[lb][2]));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const bool fixed = mask && mask[nb * 3 + d];
+#pragma unroll
+          for (int j = 0; j < L; ++j) {
+            const T xv = fixed ? T(0) : x[(nb * 3 + d) * L + j];
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              part[c * L + j] += Ks[(3 * la + c) * 24 + 3 * lb + d] * xv;
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 3 * L; ++q) acc[q] += s * part[q];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const bool fixed = mask && mask[a * 3 + c];
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int64_t idx = (a * 3 + c) * L + j;
+        const T ax = fixed ? x[idx] : acc[c * L + j];
+        T out;
+        if (MODE == 0) out = ax;
+        else if (MODE == 1) out = b[idx] - ax;
+        else out = y[idx] - ax;
+        y[idx] = out;
+        if (DOT) dacc[j] += (double)x[idx] * (double)out;
+      }
+    }
+  }
+  if (DOT) {
+    __shared__ double sh[32 * L];
+    block_sum<double, L>(dacc, sh);
+    grid_finish<double, L>(dacc, partials, counter, dot_out);
+  }
+}
+
+// Single-load variant tuned for throughput: the unit matrix sits in constant
+// memory and every loop index is a compile-time constant, so each of the 576
+// FMAs per node reads its K0 operand straight from the constant bank (no
+// shared-memory load instructions); the x of the 3x3x3 node neighbourhood is
+// loaded once into registers.  nmask packs the fixed flags of a node's three
+// DOFs in bits 0-2.
+__constant__ float c_K0f[576];
+
+__host__ __device__ constexpr int hoff(int a, int d) {
+  return d == 0 ? (0xD4 >> a) & 1 : (d == 1 ? (0xB2 >> a) & 1 : (0xE8 >> a) & 1);
+}
+
+template <int MODE, bool DOT>
+__global__ void __launch_bounds__(128)
+k_mf_apply1(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ nmask,
+            const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
+            double* partials, unsigned* counter, double* dot_out) {
+  TOPT_KERNEL_COUNT();
+  const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
+  const int nn = nx1 * ny1 * nz1;
+  double dacc[1] = {0.0};
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nn; a += gridDim.x * blockDim.x) {
+    const int iy = a % ny1;
+    const int ix = (a / ny1) % nx1;
+    const int iz = a / (ny1 * nx1);
+    float xn[27][3];
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy) {
+          const int k = (dz + 1) * 9 + (dx + 1) * 3 + (dy + 1);
+          const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+          const bool in = jx >= 0 && jy >= 0 && jz >= 0 && jx < nx1 && jy < ny1 && jz < nz1;
+          const int nb = jy + ny1 * (jx + nx1 * jz);
+          const int m = in ? (nmask ? nmask[nb] : 0) : 7;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) xn[k][c] = ((m >> c) & 1) ? 0.0f : x[nb * 3 + c];
+        }
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int la = 0; la < 8; ++la) {
+      const int cx = ix - hoff(la, 0), cy = iy - hoff(la, 1), cz = iz - hoff(la, 2);
+      const bool in = cx >= 0 && cy >= 0 && cz >= 0 && cx < g.nx && cy < g.ny && cz < g.nz;
+      const float s = in ? coef[cy + g.ny * (cx + g.nx * cz)] : 0.0f;
+      float part[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int lb = 0; lb < 8; ++lb) {
+        const int k = (hoff(lb, 2) - hoff(la, 2) + 1) * 9 + (hoff(lb, 0) - hoff(la, 0) + 1) * 3 +
+                      (hoff(lb, 1) - hoff(la, 1) + 1);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xn[k][d], part[c]);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
+    }
+    const int ma = nmask ? nmask[a] : 0;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t idx = (int64_t)a * 3 + c;
+      const float ax = ((ma >> c) & 1) ? x[idx] : acc[c];
+      float out;
+      if (MODE == 0) out = ax;
+      else if (MODE == 1) out = b[idx] - ax;
+      else out = y[idx] - ax;
+      y[idx] = out;
+      if (DOT) dacc[0] += (double)x[idx] * (double)out;
+    }
+  }
+  if (DOT) {
+    __shared__ double sh[32];
+    block_sum<double, 1>(dacc, sh);
+    grid_finish<double, 1>(dacc, partials, counter, dot_out);
+  }
+}
+
+// Inverted 3x3 diagonal blocks of the matrix-free operator (block Jacobi):
+// D_a = sum_c coef_c K0[la, la], fixed DOFs as identity rows / columns.
+template <typename T>
+__global__ void k_mf_diag_inv(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
+                              const uint8_t* __restrict__ mask, T* __restrict__ dinv) {
+  TOPT_KERNEL_COUNT();
+  const int ny1 = g.ny + 1, nx1 = g.nx + 1;
+  const int64_t nn = (int64_t)nx1 * ny1 * (g.nz + 1);
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nn;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const int ai = (int)a;  // node counts fit 32 bits: cheap index math
+    const int iy = ai % ny1;
+    const int ix = (ai / ny1) % nx1;
+    const int iz = ai / (ny1 * nx1);
+    double D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int la = 0; la < 8; ++la) {
+      const int cx = ix - c_hex_off[la][0], cy = iy - c_hex_off[la][1],
+                cz = iz - c_hex_off[la][2];
+      if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
+      const double s = (double)coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) D[c * 3 + d] += s * (double)K0[(3 * la + c) * 24 + 3 * la + d];
+    }
+    if (mask) {
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d)
+          if (mask[a * 3 + c] || mask[a * 3 + d]) D[c * 3 + d] = (c == d) ? 1.0 : 0.0;
+    }
+    const double A = D[4] * D[8] - D[5] * D[7], B = -(D[3] * D[8] - D[5] * D[6]),
+                 C = D[3] * D[7] - D[4] * D[6];
+    const double det = D[0] * A + D[1] * B + D[2] * C;
+    const double si = det != 0.0 ? 1.0 / det : 0.0;
+    T* O = dinv + a * 9;
+    O[0] = (T)(A * si);
+    O[1] = (T)(-(D[1] * D[8] - D[2] * D[7]) * si);
+    O[2] = (T)((D[1] * D[5] - D[2] * D[4]) * si);
+    O[3] = (T)(B * si);
+    O[4] = (T)((D[0] * D[8] - D[2] * D[6]) * si);
+    O[5] = (T)(-(D[0] * D[5] - D[2] * D[3]) * si);
+    O[6] = (T)(C * si);
+    O[7] = (T)(-(D[0] * D[7] - D[1] * D[6]) * si);
+    O[8] = (T)((D[0] * D[4] - D[1] * D[3]) * si);
+  }
+}
+
+// Same product for small (coarse) levels, where one thread walking a row's
+// ~27 blocks is latency-bound: one warp per row, one lane per block, then a
+// warp reduction (fixed order, deterministic).
+template <typename T, int BS, int L, int MODE, bool DOT>
+__global__ void __launch_bounds__(256)
+k_sell_spmv_warp(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
+                 const T* __restrict__ b, T* __restrict__ y, double* partials,
+                 unsigned* counter, double* dot_out) {
+  TOPT_KERNEL_COUNT();
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double dacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  for (int64_t row = w0; row < sp.nrows; row += nw) {
+    const int64_t slice = row >> 5;
+    const int r = (int)(row & 31);
+    const int64_t g0 = sp.grp_of_slice[slice];
+    const int len = sp.rowlen[row];
+    T acc[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) acc[q] = T(0);
+    for (int j = lane; j < len; j += 32) {
+      const int64_t g = g0 + j;
+      const int64_t col = sp.col[g * 32 + r];
+      const T* V = vals + g * (BS * BS * 32) + r;
+#pragma unroll
+      for (int c = 0; c < BS; ++c)
+#pragma unroll
+        for (int d = 0; d < BS; ++d) {
+          const T a = V[(c * BS + d) * 32];
+#pragma unroll
+          for (int jj = 0; jj < L; ++jj) acc[c * L + jj] += a * x[(col * BS + d) * L + jj];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) acc[q] = warp_sum(acc[q]);
+    if (lane == 0) {
+#pragma unroll
+      for (int q = 0; q < BS * L; ++q) {
+        const int64_t idx = row * BS * L + q;
+        T out;
+        if (MODE == 0) out = acc[q];
+        else if (MODE == 1) out = b[idx] - acc[q];
+        else out = y[idx] - acc[q];
+        y[idx] = out;
+        if (DOT) dacc[q % L] += (double)x[idx] * (double)out;
       }
     }
   }
@@ -456,47 +732,41 @@ struct GridT {
   const int32_t *cmx, *cmy, *cmz;
   const int32_t *c0x, *c0y, *c0z;
   const double *w1x, *w1y, *w1z;
+  // restriction: per coarse index, first fine index and 3 weights
+  const int32_t *r0x, *r0y, *r0z;
+  const float *rwx, *rwy, *rwz;
 };
 
-__device__ __forceinline__ double restrict_w(int f, int i, const int32_t* cm, int nc) {
-  const int ci = cm[i];
-  if (f == ci) return 1.0;
-  if (f < ci) {
-    if (i == 0) return 0.0;
-    const int cl = cm[i - 1];
-    return f > cl ? (double)(f - cl) / (double)(ci - cl) : 0.0;
-  }
-  if (i == nc) return 0.0;
-  const int cr = cm[i + 1];
-  return f < cr ? (double)(cr - f) / (double)(cr - ci) : 0.0;
-}
-
-// bc = P^T r  (coarse node gathers its fine support, fixed order)
+// bc = P^T r  (coarse node gathers its <= 3x3x3 fine support, fixed order)
 template <typename T, int BS, int L>
 __global__ void k_restrict(GridT g, const uint8_t* __restrict__ mask,
                            const T* __restrict__ rf, T* __restrict__ bc) {
   TOPT_KERNEL_COUNT();
-  const int64_t nnx = g.ncx + 1, nny = g.ncy + 1, nnz_ = g.ncz + 1;
-  const int64_t nc = nnx * nny * nnz_;
-  const int64_t fnx = g.nfx + 1, fny = g.nfy + 1;
-  for (int64_t I = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; I < nc;
-       I += (int64_t)gridDim.x * blockDim.x) {
-    const int iy = (int)(I % nny);
-    const int ix = (int)((I / nny) % nnx);
-    const int iz = (int)(I / (nny * nnx));
-    const int fx0 = ix > 0 ? g.cmx[ix - 1] + 1 : 0, fx1 = ix < g.ncx ? g.cmx[ix + 1] - 1 : g.nfx;
-    const int fy0 = iy > 0 ? g.cmy[iy - 1] + 1 : 0, fy1 = iy < g.ncy ? g.cmy[iy + 1] - 1 : g.nfy;
-    const int fz0 = iz > 0 ? g.cmz[iz - 1] + 1 : 0, fz1 = iz < g.ncz ? g.cmz[iz + 1] - 1 : g.nfz;
+  const int nnx = g.ncx + 1, nny = g.ncy + 1;
+  const int nc = nnx * nny * (g.ncz + 1);
+  const int fnx = g.nfx + 1, fny = g.nfy + 1;
+  for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < nc; I += gridDim.x * blockDim.x) {
+    const int iy = I % nny;
+    const int ix = (I / nny) % nnx;
+    const int iz = I / (nny * nnx);
+    const int fx0 = g.r0x[ix], fy0 = g.r0y[iy], fz0 = g.r0z[iz];
     T acc[BS * L];
 #pragma unroll
     for (int q = 0; q < BS * L; ++q) acc[q] = T(0);
-    for (int fz = fz0; fz <= fz1; ++fz) {
-      const double wz = restrict_w(fz, iz, g.cmz, g.ncz);
-      for (int fx = fx0; fx <= fx1; ++fx) {
-        const double wx = restrict_w(fx, ix, g.cmx, g.ncx) * wz;
-        for (int fy = fy0; fy <= fy1; ++fy) {
-          const T w = (T)(restrict_w(fy, iy, g.cmy, g.ncy) * wx);
-          const int64_t fn = fy + fny * (fx + fnx * (int64_t)fz);
+#pragma unroll
+    for (int kz = 0; kz < 3; ++kz) {
+      const float wz = g.rwz[iz * 3 + kz];
+      if (wz == 0.0f) continue;
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
+        const float wx = g.rwx[ix * 3 + kx] * wz;
+        if (wx == 0.0f) continue;
+#pragma unroll
+        for (int ky = 0; ky < 3; ++ky) {
+          const float wy = g.rwy[iy * 3 + ky];
+          if (wy == 0.0f) continue;
+          const T w = (T)(wy * wx);
+          const int64_t fn = (fy0 + ky) + (int64_t)fny * ((fx0 + kx) + (int64_t)fnx * (fz0 + kz));
 #pragma unroll
           for (int c = 0; c < BS; ++c) {
             if (mask && mask[fn * BS + c]) continue;
@@ -507,7 +777,7 @@ __global__ void k_restrict(GridT g, const uint8_t* __restrict__ mask,
       }
     }
 #pragma unroll
-    for (int q = 0; q < BS * L; ++q) bc[I * BS * L + q] = acc[q];
+    for (int q = 0; q < BS * L; ++q) bc[(int64_t)I * BS * L + q] = acc[q];
   }
 }
 
@@ -516,14 +786,15 @@ template <typename T, int BS, int L>
 __global__ void k_prolong_add(GridT g, const uint8_t* __restrict__ mask,
                               const T* __restrict__ xc, T* __restrict__ xf) {
   TOPT_KERNEL_COUNT();
-  const int64_t fnx = g.nfx + 1, fny = g.nfy + 1, fnz = g.nfz + 1;
-  const int64_t nf = fnx * fny * fnz;
+  const int fnx = g.nfx + 1, fny = g.nfy + 1, fnz = g.nfz + 1;
+  const int nf = fnx * fny * fnz;
   const int64_t cnx = g.ncx + 1, cny = g.ncy + 1;
-  for (int64_t F = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; F < nf;
-       F += (int64_t)gridDim.x * blockDim.x) {
-    const int fy = (int)(F % fny);
-    const int fx = (int)((F / fny) % fnx);
-    const int fz = (int)(F / (fny * fnx));
+  for (int F32 = blockIdx.x * blockDim.x + threadIdx.x; F32 < nf;
+       F32 += gridDim.x * blockDim.x) {
+    const int64_t F = F32;
+    const int fy = F32 % fny;
+    const int fx = (F32 / fny) % fnx;
+    const int fz = F32 / (fny * fnx);
     const int cx = g.c0x[fx], cy = g.c0y[fy], cz = g.c0z[fz];
     const double ax = g.w1x[fx], ay = g.w1y[fy], az = g.w1z[fz];
     T acc[BS * L];
@@ -564,8 +835,6 @@ __global__ void k_prolong_add(GridT g, const uint8_t* __restrict__ mask,
 // local order) to e's nodes.  One CTA per coarse cell; fine elements are the
 // hex cells of the finer grid (cell_ptr == nullptr) or the elements listed
 // per fine cell.
-__constant__ int c_hex_off[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1},
-                                    {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 1}};
 
 template <typename T, int BS, int NLOC>
 __global__ void __launch_bounds__(256)

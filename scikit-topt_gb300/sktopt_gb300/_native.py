@@ -43,6 +43,7 @@ class FemDesc(C.Structure):
         ("grid", C.c_int32 * 3), ("node_ijk", C.POINTER(C.c_int32)),
         ("cell_of_elem", C.POINTER(C.c_int32)),
         ("mixed", C.c_int32), ("mg_levels", C.c_int32), ("mg_coarse_max", C.c_int32),
+        ("mf_level0", C.c_int32),
     ]
 
 

@@ -33,7 +33,7 @@ class FemEngine:
 
     def __init__(self, mesh: GridMesh, bs: int, ke: np.ndarray, dirichlet_mask: np.ndarray,
                  mixed: bool = False, multigrid: bool = True, mg_levels: int = 16,
-                 mg_coarse_max: int = 200, device=None):
+                 mg_coarse_max: int = 200, device=None, matrix_free: bool = True):
         self.lib = N.load()
         self.device = device or default_device()
         self.mesh = mesh
@@ -66,6 +66,7 @@ class FemEngine:
         d.mixed = 1 if mixed else 0
         d.mg_levels = mg_levels if multigrid else 1
         d.mg_coarse_max = mg_coarse_max
+        d.mf_level0 = 1 if matrix_free else 0
         h = C.c_void_p()
         with torch.cuda.device(self.device):
             N.check(self.lib.topt_fem_create(C.byref(d), C.byref(h)))
