@@ -187,13 +187,18 @@ int topt_projection(int64_t n, const double* x, double beta, double eta,
  * its design entries replaced by the accepted candidate; vol: design-element
  * volumes (design order).  scaling (design order, may be NULL) receives the
  * clipped multiplicative factor; lmid, vol_error, steps (host) the
- * bisection result. */
+ * bisection result.  Unless flags has TOPT_OC_EXACT, each step first
+ * evaluates the volume in FP32 and re-evaluates it in FP64 only when the
+ * FP32 error is within its rounding bound of a decision edge (0 or vol_tol),
+ * so the sequence of brackets, the result and vol_error are those of the
+ * all-FP64 bisection. */
 typedef struct topt_oc_params {
   double rho_min, rho_max, move_limit, eta, eps, vol_frac, beta, beta_eta;
   double scaling_min, scaling_max, vol_tol, l1, l2, tolerance;
   int32_t max_iter;
-  int32_t pad;
+  int32_t flags;   /* TOPT_OC_EXACT: evaluate every bisection step in FP64 */
 } topt_oc_params;
+#define TOPT_OC_EXACT 1
 int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rho,
                    const double* vol, double vol_sum, const topt_oc_params* prm,
                    double* scaling, double* lmid, double* vol_error, int32_t* steps);

@@ -48,6 +48,8 @@ struct LevelNum {
   DevBuf vals, dinv;
   DevBuf b, x, r, d, q;
   DevBuf dense_inv;
+  DevBuf pw;              // power-iteration vector (unit norm once pw_ready)
+  bool pw_ready = false;
   double lmax = 0.0;
 };
 
@@ -214,7 +216,7 @@ static int make_transfer(LevelStruct& F, const LevelStruct& Cs, cudaStream_t s) 
   std::vector<int32_t> cm[3] = {coarse_map(F.nx), coarse_map(F.ny), coarse_map(F.nz)};
   int nf[3] = {F.nx, F.ny, F.nz};
   std::vector<int32_t> c0[3];
-  std::vector<double> w1[3];
+  std::vector<float> w1[3];
   for (int d = 0; d < 3; ++d) {
     const int nc = (int)cm[d].size() - 1;
     c0[d].resize(nf[d] + 1);
@@ -223,7 +225,7 @@ static int make_transfer(LevelStruct& F, const LevelStruct& Cs, cudaStream_t s) 
     for (int f = 0; f <= nf[d]; ++f) {
       while (i + 1 < nc && cm[d][i + 1] <= f) ++i;
       c0[d][f] = i;
-      w1[d][f] = (double)(f - cm[d][i]) / (double)(cm[d][i + 1] - cm[d][i]);
+      w1[d][f] = (float)(f - cm[d][i]) / (float)(cm[d][i + 1] - cm[d][i]);
     }
   }
   int rc;
@@ -242,7 +244,7 @@ static int make_transfer(LevelStruct& F, const LevelStruct& Cs, cudaStream_t s) 
   g.ncx = Cs.nx; g.ncy = Cs.ny; g.ncz = Cs.nz;
   g.cmx = F.cmx.as<int32_t>(); g.cmy = F.cmy.as<int32_t>(); g.cmz = F.cmz.as<int32_t>();
   g.c0x = F.c0x.as<int32_t>(); g.c0y = F.c0y.as<int32_t>(); g.c0z = F.c0z.as<int32_t>();
-  g.w1x = F.w1x.as<double>(); g.w1y = F.w1y.as<double>(); g.w1z = F.w1z.as<double>();
+  g.w1x = F.w1x.as<float>(); g.w1y = F.w1y.as<float>(); g.w1z = F.w1z.as<float>();
   // restriction tables: coarse node i gathers fine nodes r0[i] + k, k < 3,
   // with the hat weights of its interpolation (P^T row)
   std::vector<int32_t> r0[3];
@@ -299,21 +301,35 @@ static int assemble(topt_fem* h, const LevelStruct& L, int bs, int nloc, const T
   return fail(TOPT_BAD_INPUT, "assemble: unsupported bs/nloc");
 }
 
+// Coarse-level product shapes by level size: one warp per block row up to
+// kWarpRowsMax rows, three threads per row (3x3 blocks) up to kRow3Max, one
+// thread per row above.
+static const int64_t kWarpRowsMax = 16384;
+static const int64_t kRow3Max = 131072;
+
 template <typename T, int BS, int L, int MODE, bool DOT>
 static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const T* x,
-                       const T* b, T* y, int red_slot) {
-  if (Ls.n_nodes <= 65536) {   // coarse levels: one warp per row
+                       const T* b, T* y, int red_slot, const ChebEp<T>& ep) {
+  if (BS == 3 && Ls.n_nodes > kWarpRowsMax && Ls.n_nodes <= kRow3Max) {
+    const int g = grid_for((Ls.n_nodes + 63) / 64, 1, h->sm * 16);
+    k_sell_spmv3<T, L, MODE, DOT><<<g, 192, 0, h->stream>>>(
+        Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
+        h->red.res(red_slot), ep);
+    TOPT_CHECK_LAUNCH("k_sell_spmv3");
+    return TOPT_OK;
+  }
+  if (Ls.n_nodes <= kWarpRowsMax) {
     const int g = gridsize(h, Ls.n_nodes * 32);
     k_sell_spmv_warp<T, BS, L, MODE, DOT><<<g, kBlock, 0, h->stream>>>(
         Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
-        h->red.res(red_slot));
+        h->red.res(red_slot), ep);
     TOPT_CHECK_LAUNCH("k_sell_spmv_warp");
     return TOPT_OK;
   }
   const int g = gridsize(h, Ls.n_nodes);
   k_sell_spmv<T, BS, L, MODE, DOT><<<g, kBlock, 0, h->stream>>>(
       Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
-      h->red.res(red_slot));
+      h->red.res(red_slot), ep);
   TOPT_CHECK_LAUNCH("k_sell_spmv");
   return TOPT_OK;
 }
@@ -325,34 +341,35 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 static const void* g_k0_owner = nullptr;
 
 template <int L, int MODE, bool DOT>
-static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot,
+                     const ChebEp<float>& ep) {
   if (L == 1) {
     if (g_k0_owner != h->ke32.p) {
       TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->ke32.p, 576 * sizeof(float), 0,
                                         cudaMemcpyDeviceToDevice, h->stream));
       g_k0_owner = h->ke32.p;
     }
-    k_mf_apply1<MODE, DOT><<<gridsize(h, h->n_nodes, 128), 128, 0, h->stream>>>(
+    k_mf_tile<MODE, DOT><<<(int)mf_tiles(h->mfg), kMfThreads, 0, h->stream>>>(
         h->mfg, h->coef32.as<float>(), h->nmask.as<uint8_t>(), x, b, y,
-        h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
-    TOPT_CHECK_LAUNCH("k_mf_apply1");
+        h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot), ep);
+    TOPT_CHECK_LAUNCH("k_mf_tile");
     return TOPT_OK;
   }
   k_mf_apply<float, L, MODE, DOT><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
       h->mfg, h->ke32.as<float>(), h->coef32.as<float>(), h->mask.as<uint8_t>(), x, b, y,
-      h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
+      h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot), ep);
   TOPT_CHECK_LAUNCH("k_mf_apply");
   return TOPT_OK;
 }
 
 static int mf_spmv(topt_fem* h, int L, int mode, bool dot, const float* x, const float* b,
-                   float* y, int slot) {
-#define TOPT_MF_CASE(L_)                                                          \
-  if (L == L_) {                                                                  \
-    if (mode == 0 && !dot) return launch_mf<L_, 0, false>(h, x, b, y, slot);      \
-    if (mode == 0 && dot) return launch_mf<L_, 0, true>(h, x, b, y, slot);        \
-    if (mode == 1) return launch_mf<L_, 1, false>(h, x, b, y, slot);              \
-    if (mode == 2) return launch_mf<L_, 2, false>(h, x, b, y, slot);              \
+                   float* y, int slot, const ChebEp<float>& ep) {
+#define TOPT_MF_CASE(L_)                                                            \
+  if (L == L_) {                                                                    \
+    if (mode == 0 && !dot) return launch_mf<L_, 0, false>(h, x, b, y, slot, ep);    \
+    if (mode == 0 && dot) return launch_mf<L_, 0, true>(h, x, b, y, slot, ep);      \
+    if (mode == 1) return launch_mf<L_, 1, false>(h, x, b, y, slot, ep);            \
+    if (mode == 2) return launch_mf<L_, 2, false>(h, x, b, y, slot, ep);            \
   }
   TOPT_MF_CASE(1) TOPT_MF_CASE(2) TOPT_MF_CASE(3) TOPT_MF_CASE(4)
 #undef TOPT_MF_CASE
@@ -361,15 +378,19 @@ static int mf_spmv(topt_fem* h, int L, int mode, bool dot, const float* x, const
 
 template <typename T>
 static int spmv(topt_fem* h, const LevelStruct& Ls, int bs, int L, int mode, bool dot,
-                const T* vals, const T* x, const T* b, T* y, int slot = 0) {
+                const T* vals, const T* x, const T* b, T* y, int slot = 0,
+                const ChebEp<T>& ep = ChebEp<T>()) {
   if (std::is_same<T, float>::value && h->mf && &Ls == &h->ls[0])
-    return mf_spmv(h, L, mode, dot, (const float*)x, (const float*)b, (float*)y, slot);
+    return mf_spmv(h, L, mode, dot, (const float*)x, (const float*)b, (float*)y, slot,
+                   reinterpret_cast<const ChebEp<float>&>(ep));
 #define TOPT_SPMV_CASE(BS_, L_)                                                        \
   if (bs == BS_ && L == L_) {                                                          \
-    if (mode == 0 && !dot) return launch_spmv<T, BS_, L_, 0, false>(h, Ls, vals, x, b, y, slot); \
-    if (mode == 0 && dot) return launch_spmv<T, BS_, L_, 0, true>(h, Ls, vals, x, b, y, slot);   \
-    if (mode == 1) return launch_spmv<T, BS_, L_, 1, false>(h, Ls, vals, x, b, y, slot);         \
-    if (mode == 2) return launch_spmv<T, BS_, L_, 2, false>(h, Ls, vals, x, b, y, slot);         \
+    if (mode == 0 && !dot)                                                             \
+      return launch_spmv<T, BS_, L_, 0, false>(h, Ls, vals, x, b, y, slot, ep);        \
+    if (mode == 0 && dot)                                                              \
+      return launch_spmv<T, BS_, L_, 0, true>(h, Ls, vals, x, b, y, slot, ep);         \
+    if (mode == 1) return launch_spmv<T, BS_, L_, 1, false>(h, Ls, vals, x, b, y, slot, ep); \
+    if (mode == 2) return launch_spmv<T, BS_, L_, 2, false>(h, Ls, vals, x, b, y, slot, ep); \
   }
   TOPT_SPMV_CASE(3, 1) TOPT_SPMV_CASE(3, 2) TOPT_SPMV_CASE(3, 3) TOPT_SPMV_CASE(3, 4)
   TOPT_SPMV_CASE(1, 1) TOPT_SPMV_CASE(1, 2) TOPT_SPMV_CASE(1, 3) TOPT_SPMV_CASE(1, 4)
@@ -437,6 +458,7 @@ static int alloc_level_num(topt_fem* h, LevelNum<T>& N, const LevelStruct& L, in
   if ((rc = N.dinv.alloc(sizeof(T) * L.n_nodes * bs * bs))) return rc;
   for (DevBuf* b : {&N.b, &N.x, &N.r, &N.d, &N.q})
     if ((rc = b->alloc(sizeof(T) * nd * 4))) return rc;
+  if (!L.dense && (rc = N.pw.alloc(sizeof(T) * nd))) return rc;
   if (L.dense) {
     if ((rc = N.dense_inv.alloc(sizeof(T) * (size_t)L.ndense * L.ndense))) return rc;
   }
@@ -590,20 +612,22 @@ static int block_inv(topt_fem* h, const LevelStruct& L, const T* vals, T* dinv, 
   return TOPT_OK;
 }
 
-// lambda_max(D^-1 A) by power iteration (10 steps, 1.1 safety factor).
+// lambda_max(D^-1 A) by power iteration with a 1.1 safety factor.  The unit
+// iterate is kept per level and warm-starts the next refresh of the same
+// handle (the operator changes little between design updates): 10 steps on
+// the first refresh, 4 afterwards.  No host round trip until the end.
 template <typename T>
 static int estimate_lmax(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, double* out) {
   const int bs = h->bs;
   const int64_t nd = L.n_nodes * bs;
-  T* v = N.d.template as<T>();
+  T* v = N.pw.template as<T>();
   T* w = N.q.template as<T>();
-  k_hash_fill<T><<<gridsize(h, nd), kBlock, 0, h->stream>>>(nd, v);
-  double nv = 0.0, lam = 0.0;
+  T* tmp = N.r.template as<T>();
+  const int iters = N.pw_ready ? 4 : 10;
+  if (!N.pw_ready) k_hash_fill<T><<<gridsize(h, nd), kBlock, 0, h->stream>>>(nd, v);
   int rc;
-  if ((rc = dot<T>(h, nd, 1, v, v, 1))) return rc;
-  if ((rc = read_slot(h, 1, 1, &nv))) return rc;
-  for (int it = 0; it < 10; ++it) {
-    T* tmp = N.r.template as<T>();
+  for (int it = 0; it < iters; ++it) {
+    if (it == iters - 1 && (rc = dot<T>(h, nd, 1, v, v, 1))) return rc;
     if ((rc = spmv<T>(h, L, bs, 1, 0, false, N.vals.template as<T>(), v, nullptr, tmp))) return rc;
     if (bs == 3)
       k_block_jacobi<T, 3, 1, false><<<gridsize(h, L.n_nodes), kBlock, 0, h->stream>>>(
@@ -611,15 +635,19 @@ static int estimate_lmax(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, doub
     else
       k_block_jacobi<T, 1, 1, false><<<gridsize(h, L.n_nodes), kBlock, 0, h->stream>>>(
           L.n_nodes, N.dinv.template as<T>(), tmp, w, nullptr, nullptr, nullptr);
-    double nw = 0.0;
-    if ((rc = dot<T>(h, nd, 1, w, w, 1))) return rc;
-    if ((rc = read_slot(h, 1, 1, &nw))) return rc;
-    if (!(nw > 0.0) || !std::isfinite(nw)) break;
-    lam = std::sqrt(nw / nv);
-    // v = w / |w| (scaled to unit norm)
-    k_convert<T, T><<<gridsize(h, nd), kBlock, 0, h->stream>>>(nd, w, v);
-    nv = nw;
+    if (it < iters - 1) k_convert<T, T><<<gridsize(h, nd), kBlock, 0, h->stream>>>(nd, w, v);
   }
+  if ((rc = dot<T>(h, nd, 1, w, w, 11))) return rc;
+  double nv = 0.0, nw = 0.0;
+  if ((rc = read_slot(h, 1, 1, &nv))) return rc;
+  if ((rc = read_slot(h, 11, 1, &nw))) return rc;
+  const bool ok = nw > 0.0 && nv > 0.0 && std::isfinite(nw) && std::isfinite(nv);
+  const double lam = ok ? std::sqrt(nw / nv) : 0.0;
+  if (ok) {
+    k_scale<T><<<gridsize(h, nd), kBlock, 0, h->stream>>>(nd, (T)(1.0 / std::sqrt(nw)), w, v);
+    TOPT_CHECK_LAUNCH("k_scale");
+  }
+  N.pw_ready = ok;
   *out = lam > 0.0 ? 1.1 * lam : 2.0;
   return TOPT_OK;
 }
@@ -643,6 +671,18 @@ static int build_dense(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, DevBuf
   TOPT_CUDA(cudaStreamSynchronize(h->stream));
   return TOPT_OK;
 }
+
+// Chebyshev smoothing (Saad, Iterative Methods, Alg. 12.1) on the interval
+// [lmax/30, lmax] of Dinv A.
+struct ChebParams {
+  double theta, delta, sigma;
+  explicit ChebParams(double lmax) {
+    const double lmin = lmax / 30.0;
+    theta = 0.5 * (lmax + lmin);
+    delta = 0.5 * (lmax - lmin);
+    sigma = theta / delta;
+  }
+};
 
 // Rebuild level values (level 0 from coef) and the hierarchy of precision T.
 template <typename T>
@@ -696,101 +736,154 @@ static int refresh(topt_fem* h, Hier<T>& H) {
 }
 
 // ---------------------------------------------------------------- V-cycle
+// Chebyshev smoothing (ChebParams): every step after the first runs fused
+// into the operator application that produces its residual (ChebEp); the
+// search directions d ping-pong between N.d and N.q.
+
+// Pre-smoothing from a zero guess.  On entry the first step is applied
+// (N.d = x = Dinv b / theta, by the restriction or the V-cycle start); on
+// exit N.r = b - A x.
 template <typename T>
-static int cheb_smooth(topt_fem* h, int li, Hier<T>& H, int L, int degree, bool x_zero,
-                       bool need_residual) {
+static int smooth_pre(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b, T* x) {
   LevelStruct& Ls = h->ls[li];
   LevelNum<T>& N = H.lv[li];
-  const int bs = h->bs;
-  const double lmax = N.lmax, lmin = lmax / 30.0;
-  const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin);
-  const double sigma = theta / delta;
-  double rho0 = 1.0 / sigma;
+  const ChebParams cp(N.lmax);
+  double rho0 = 1.0 / cp.sigma;
   T* r = N.r.template as<T>();
-  T* d = N.d.template as<T>();
-  T* x = N.x.template as<T>();
-  const T* dinv = N.dinv.template as<T>();
+  T* dA = N.d.template as<T>();
+  T* dB = N.q.template as<T>();
   const T* vals = N.vals.template as<T>();
   int rc;
-  const int g = gridsize(h, Ls.n_nodes);
-  TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<g, kBlock, 0, h->stream>>>(
-                               Ls.n_nodes, dinv, r, d, x, T(0), (T)(1.0 / theta), 1,
-                               x_zero ? 1 : 0)));
+  ChebEp<T> ep;
+  ep.dinv = N.dinv.template as<T>();
+  ep.x = x;
+  ep.kind = 2;
   for (int k = 1; k < degree; ++k) {
-    if ((rc = spmv<T>(h, Ls, bs, L, 2, false, vals, d, nullptr, r))) return rc;
-    const double rho1 = 1.0 / (2.0 * sigma - rho0);
-    const T c1 = (T)(rho1 * rho0), c2 = (T)(2.0 * rho1 / delta);
-    TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<g, kBlock, 0, h->stream>>>(
-                                 Ls.n_nodes, dinv, r, d, x, c1, c2, 0, 0)));
+    const double rho1 = 1.0 / (2.0 * cp.sigma - rho0);
+    ep.c1 = (T)(rho1 * rho0);
+    ep.c2 = (T)(2.0 * rho1 / cp.delta);
+    ep.dold = dA;
+    ep.dnew = dB;
+    // step 1: r = b - A d (x == d); later steps: r -= A d
+    if ((rc = spmv<T>(h, Ls, h->bs, L, k == 1 ? 1 : 2, false, vals, dA, b, r, 0, ep))) return rc;
+    std::swap(dA, dB);
     rho0 = rho1;
   }
-  if (need_residual) {
-    if ((rc = spmv<T>(h, Ls, bs, L, 2, false, vals, d, nullptr, r))) return rc;
+  return spmv<T>(h, Ls, h->bs, L, degree == 1 ? 1 : 2, false, vals, dA, b, r);
+}
+
+// Post-smoothing of x (nonzero guess): r = b - A x fused with the first
+// step d = Dinv r / theta, then degree-1 fused steps that update x.
+template <typename T>
+static int smooth_post(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b, T* x) {
+  LevelStruct& Ls = h->ls[li];
+  LevelNum<T>& N = H.lv[li];
+  const ChebParams cp(N.lmax);
+  double rho0 = 1.0 / cp.sigma;
+  T* r = N.r.template as<T>();
+  T* dA = N.d.template as<T>();
+  T* dB = N.q.template as<T>();
+  const T* vals = N.vals.template as<T>();
+  const int64_t nl = Ls.n_nodes * h->bs * L;
+  int rc;
+  ChebEp<T> ep;
+  ep.dinv = N.dinv.template as<T>();
+  ep.kind = 1;
+  ep.c2 = (T)(1.0 / cp.theta);
+  ep.dnew = dA;
+  if ((rc = spmv<T>(h, Ls, h->bs, L, 1, false, vals, x, b, r, 0, ep))) return rc;
+  if (degree == 1) {
+    k_axpy<T><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, T(1), dA, x);
+    TOPT_CHECK_LAUNCH("k_axpy");
+    return TOPT_OK;
   }
-  TOPT_CHECK_LAUNCH("k_cheb");
+  ep.kind = 2;
+  ep.x = x;
+  for (int k = 1; k < degree; ++k) {
+    const double rho1 = 1.0 / (2.0 * cp.sigma - rho0);
+    ep.c1 = (T)(rho1 * rho0);
+    ep.c2 = (T)(2.0 * rho1 / cp.delta);
+    ep.dold = dA;
+    ep.dnew = dB;
+    ep.add_old = (k == 1);
+    if ((rc = spmv<T>(h, Ls, h->bs, L, 2, false, vals, dA, nullptr, r, 0, ep))) return rc;
+    std::swap(dA, dB);
+    rho0 = rho1;
+  }
   return TOPT_OK;
 }
 
-// Solve approximately A_li x = b_li (b in N.b, x to N.x).  N.r is clobbered.
+// x ~= A_li^-1 b.  started: the first smoothing step is already applied
+// (coarse levels: by the restriction that produced b).
 template <typename T>
-static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree) {
+static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b, T* x,
+                  bool started) {
   LevelStruct& Ls = h->ls[li];
   LevelNum<T>& N = H.lv[li];
   const int bs = h->bs;
-  const int64_t nd = Ls.n_nodes * bs;
   int rc;
   if (Ls.dense) {
     const int n = Ls.ndense;
     TOPT_L_DISPATCH(L, (k_dense_matvec<T, L_><<<grid_for((int64_t)n * 32, 256), 256, 0,
                                                   h->stream>>>(n, N.dense_inv.template as<T>(),
-                                                               N.b.template as<T>(),
-                                                               N.x.template as<T>())));
+                                                               b, x)));
     TOPT_CHECK_LAUNCH("k_dense_matvec");
     return TOPT_OK;
   }
-  // r = b
-  TOPT_CUDA(cudaMemcpyAsync(N.r.p, N.b.p, sizeof(T) * nd * L, cudaMemcpyDeviceToDevice,
-                            h->stream));
-  if ((rc = cheb_smooth<T>(h, li, H, L, degree, true, true))) return rc;
+  if (!started) {
+    const ChebParams cp(N.lmax);
+    TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
+                                                  h->stream>>>(
+                                 Ls.n_nodes, N.dinv.template as<T>(), b, N.d.template as<T>(),
+                                 x, T(0), (T)(1.0 / cp.theta), 1, 1)));
+    TOPT_CHECK_LAUNCH("k_cheb");
+  }
+  if ((rc = smooth_pre<T>(h, li, H, L, degree, b, x))) return rc;
   LevelNum<T>& C = H.lv[li + 1];
+  const LevelStruct& Cs = h->ls[li + 1];
   const uint8_t* mask = li == 0 ? h->mask.as<uint8_t>() : nullptr;
-  const int64_t ncn = h->ls[li + 1].n_nodes;
-  TOPT_BSL_DISPATCH(bs, L, (k_restrict<T, BS_, L_><<<gridsize(h, ncn), kBlock, 0, h->stream>>>(
-                               Ls.grid, mask, N.r.template as<T>(), C.b.template as<T>())));
+  const T c2c = Cs.dense ? T(0) : (T)(1.0 / ChebParams(C.lmax).theta);
+  const T* dinv_c = Cs.dense ? nullptr : C.dinv.template as<T>();
+  TOPT_BSL_DISPATCH(bs, L, (k_restrict<T, BS_, L_><<<gridsize(h, Cs.n_nodes), kBlock, 0,
+                                                     h->stream>>>(
+                               Ls.grid, mask, N.r.template as<T>(), C.b.template as<T>(), dinv_c,
+                               C.d.template as<T>(), C.x.template as<T>(), c2c)));
   TOPT_CHECK_LAUNCH("k_restrict");
-  if ((rc = vcycle<T>(h, li + 1, H, L, degree))) return rc;
+  if ((rc = vcycle<T>(h, li + 1, H, L, degree, C.b.template as<T>(), C.x.template as<T>(), true)))
+    return rc;
   TOPT_BSL_DISPATCH(bs, L, (k_prolong_add<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
                                                          h->stream>>>(
-                               Ls.grid, mask, C.x.template as<T>(), N.x.template as<T>())));
+                               Ls.grid, mask, C.x.template as<T>(), x)));
   TOPT_CHECK_LAUNCH("k_prolong_add");
-  // r = b - A x, post-smooth
-  if ((rc = spmv<T>(h, Ls, bs, L, 1, false, N.vals.template as<T>(), N.x.template as<T>(),
-                    N.b.template as<T>(), N.r.template as<T>())))
-    return rc;
-  return cheb_smooth<T>(h, li, H, L, degree, false, false);
+  return smooth_post<T>(h, li, H, L, degree, b, x);
 }
 
 // ---------------------------------------------------------------- PCG
-// z = M^-1 r (V-cycle or block Jacobi) and r.z into reducer slot `slot`.
+// z = M^-1 r (V-cycle or block Jacobi); r.z into reducer slot `slot` unless
+// slot < 0.
 template <typename T>
 static int precond_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int precond,
                          int degree, int slot) {
   LevelStruct& L0 = h->ls[0];
   LevelNum<T>& N0 = H.lv[0];
   const int bs = h->bs;
-  const int64_t nl = h->n_dof * L;
   if (precond == 1 && h->ls.size() > 1) {
-    TOPT_CUDA(cudaMemcpyAsync(N0.b.p, r, sizeof(T) * nl, cudaMemcpyDeviceToDevice, h->stream));
-    int rc2 = vcycle<T>(h, 0, H, L, degree);
+    int rc2 = vcycle<T>(h, 0, H, L, degree, r, z, false);
     if (rc2) return rc2;
-    TOPT_CUDA(cudaMemcpyAsync(z, N0.x.p, sizeof(T) * nl, cudaMemcpyDeviceToDevice, h->stream));
-    return dot<T>(h, h->n_dof, L, r, z, slot);
+    return slot < 0 ? TOPT_OK : dot<T>(h, h->n_dof, L, r, z, slot);
   }
-  TOPT_BSL_DISPATCH(bs, L, (k_block_jacobi<T, BS_, L_, true><<<gridsize(h, L0.n_nodes), kBlock,
-                                                                0, h->stream>>>(
-                               L0.n_nodes, N0.dinv.template as<T>(), r, z,
-                               h->red.partials.as<double>(), h->red.ctr(slot),
-                               h->red.res(slot))));
+  if (slot < 0) {
+    TOPT_BSL_DISPATCH(bs, L, (k_block_jacobi<T, BS_, L_, false><<<gridsize(h, L0.n_nodes),
+                                                                   kBlock, 0, h->stream>>>(
+                                 L0.n_nodes, N0.dinv.template as<T>(), r, z, nullptr, nullptr,
+                                 nullptr)));
+  } else {
+    TOPT_BSL_DISPATCH(bs, L, (k_block_jacobi<T, BS_, L_, true><<<gridsize(h, L0.n_nodes),
+                                                                  kBlock, 0, h->stream>>>(
+                                 L0.n_nodes, N0.dinv.template as<T>(), r, z,
+                                 h->red.partials.as<double>(), h->red.ctr(slot),
+                                 h->red.res(slot))));
+  }
   TOPT_CHECK_LAUNCH("k_block_jacobi");
   return TOPT_OK;
 }
@@ -827,7 +920,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
   k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
   int slot_old = 3, slot_new = 4;
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, slot_new))) return rc;
-  TOPT_L_DISPATCH(L, (k_pcg_direction<float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+  TOPT_L_DISPATCH(L, (k_pcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                          n, h->red.res(slot_new), h->red.res(slot_old), 1, z32, p32)));
   std::swap(slot_old, slot_new);
   inf->status = TOPT_MAXITER;
@@ -839,7 +932,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
     TOPT_L_DISPATCH(L, (k_pcg_update<float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p32, q32,
                            x32, r32, h->red.partials.as<double>(), h->red.ctr(6),
-                           h->red.res(6))));
+                           h->red.res(6), nullptr)));
     TOPT_CHECK_LAUNCH("k_pcg_update");
     inf->iters = it;
     if ((rc = read_slot(h, 6, L, rr))) return rc;
@@ -877,7 +970,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
       k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, R, r32);
     }
     if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, slot_new))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_direction<float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_pcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_new), h->red.res(slot_old), 0, z32, p32)));
     std::swap(slot_old, slot_new);
   }
@@ -915,7 +1008,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
     return precond_apply<T>(h, H, L, r, z, precond, degree, slot);
   };
   if ((rc = apply_prec(slot_new))) return rc;
-  TOPT_L_DISPATCH(L, (k_pcg_direction<T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+  TOPT_L_DISPATCH(L, (k_pcg_direction<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                          n, h->red.res(slot_new), h->red.res(slot_old), 1, z, p)));
   std::swap(slot_old, slot_new);
   int it = 0;
@@ -927,7 +1020,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
     if ((rc = spmv<T>(h, L0, bs, L, 0, true, vals, p, nullptr, q, 5))) return rc;
     TOPT_L_DISPATCH(L, (k_pcg_update<T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p, q, x, r,
-                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6))));
+                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), nullptr)));
     TOPT_CHECK_LAUNCH("k_pcg_update");
     if (it % check_every == 0 || it == maxiter) {
       if ((rc = read_slot(h, 6, L, rr))) return rc;
@@ -944,7 +1037,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
       if (done) { *status = TOPT_OK; break; }
     }
     if ((rc = apply_prec(slot_new))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_direction<T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_pcg_direction<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_new), h->red.res(slot_old), 0, z, p)));
     std::swap(slot_old, slot_new);
   }
@@ -958,10 +1051,12 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
 // residual, solution update, dots) whose preconditioner -- the inner solve --
 // is one FP32 multigrid V-cycle (or FP32 block Jacobi) applied to the
 // rounded FP64 residual.  The Polak-Ribiere direction update keeps CG
-// convergence although the FP32 inner solve is not exactly linear.
-static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, double* z,
-                         double* r, float* r32, float* z32, double rtol, int maxiter,
-                         int precond, int degree, int check_every, topt_solve_info* inf) {
+// convergence although the FP32 inner solve is not exactly linear.  The FP32
+// copy of r is written by the residual update itself and z stays FP32 (the
+// direction and dot kernels widen it on load).
+static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, double* r,
+                         float* r32, float* z32, double rtol, int maxiter, int precond,
+                         int degree, int check_every, topt_solve_info* inf) {
   Hier<float>& H = h->h32;
   LevelStruct& L0 = h->ls[0];
   const int bs = h->bs;
@@ -979,28 +1074,27 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   if ((rc = upload(active, active_h, 4, h->stream))) return rc;
   TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
   TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice, h->stream));
-  // z = M32(r) ; slot 3 <- r.z
-  auto inner = [&]() -> int {
-    k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r, r32);
-    int rc2 = precond_apply<float>(h, H, L, r32, z32, precond, degree, 9);
-    if (rc2) return rc2;
-    k_convert<double, float><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, z32, z);
-    TOPT_CHECK_LAUNCH("k_convert");
-    return TOPT_OK;
-  };
-  if ((rc = inner())) return rc;
-  if ((rc = dot<double>(h, n, L, r, z, 3))) return rc;
-  TOPT_L_DISPATCH(L, (k_pcg_direction<double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                         n, h->red.res(3), h->red.res(3), 1, z, p)));
+  k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
+  TOPT_CHECK_LAUNCH("k_convert");
+  // z = M32(r); slot 3 <- r.z (FP64 r, FP32 z)
+  if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
+  TOPT_L_DISPATCH(L, (k_dot2<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                         n, r, r, z32, h->red.partials.as<double>(), h->red.ctr(8),
+                         h->red.res(8))));
+  TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
+                            cudaMemcpyDeviceToDevice, h->stream));
+  TOPT_L_DISPATCH(L, (k_pcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                           h->stream>>>(
+                         n, h->red.res(3), h->red.res(3), 1, z32, p)));
   inf->status = TOPT_MAXITER;
   double rel = 1.0;
   int it;
   for (it = 1; it <= maxiter; ++it) {
-    // q = A p, pq = p.q (slot 5); x += a p, r -= a q, rr (slot 6)
+    // q = A p, pq = p.q (slot 5); x += a p, r -= a q, r32 = float(r), rr (slot 6)
     if ((rc = spmv<double>(h, L0, bs, L, 0, true, A64, p, nullptr, q, 5))) return rc;
     TOPT_L_DISPATCH(L, (k_pcg_update<double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(3), h->red.res(5), active.as<int>(), p, q, U, r,
-                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6))));
+                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), r32)));
     TOPT_CHECK_LAUNCH("k_pcg_update");
     if (it % check_every == 0 || it == maxiter) {
       if ((rc = read_slot(h, 6, L, rr))) return rc;
@@ -1016,13 +1110,14 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
       if (bad) { inf->status = TOPT_NONFINITE; break; }
       if (done) { inf->status = TOPT_OK; break; }
     }
-    if ((rc = inner())) return rc;
-    // slot 3 <- r.z_new, slot 8 <- q.z_new
-    TOPT_L_DISPATCH(L, (k_dot2<double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                           n, r, q, z, h->red.partials.as<double>(), h->red.ctr(8),
+    if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
+    // slot 8 <- (r.z_new, q.z_new); slot 3 <- r.z_new
+    TOPT_L_DISPATCH(L, (k_dot2<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                           n, r, q, z32, h->red.partials.as<double>(), h->red.ctr(8),
                            h->red.res(8))));
-    TOPT_L_DISPATCH(L, (k_fcg_direction<double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z, p)));
+    TOPT_L_DISPATCH(L, (k_fcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                             h->stream>>>(
+                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p)));
     TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
                               cudaMemcpyDeviceToDevice, h->stream));
     TOPT_CHECK_LAUNCH("k_fcg_direction");
@@ -1141,6 +1236,10 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
                           (d->dirichlet[3 * n + 2] ? 4 : 0));
       if ((rc = upload(h->nmask, nm.data(), nm.size(), s))) return rc;
       TOPT_CUDA(cudaStreamSynchronize(s));
+      // one grid-reduction partial per tile of the fused p.Ap variant
+      if (mf_tiles(h->mfg) > h->red.max_blocks &&
+          (rc = h->red.init((int)std::min<int64_t>(mf_tiles(h->mfg), INT32_MAX / 8))))
+        return rc;
     }
     if (h->ls.size() > 1) {
       LevelStruct& B = h->ls.back();
@@ -1271,11 +1370,11 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
                           o->precond, degree, check, &inf.iters, &inf.relres, &inf.status)))
       return rc;
   } else if (o->method == 3) {
-    // FP64 flexible CG, FP32 multigrid inner solve; U0 holds p, q, z, r (FP64)
+    // FP64 flexible CG, FP32 multigrid inner solve; U0 holds p, q, r (FP64)
     // and R holds the FP32 r and z.
     float* r32 = (float*)h->R.p;
-    if ((rc = pcg_fcg_mixed(h, L, U, p, q, z, r, r32, r32 + nl, o->rtol, o->maxiter,
-                            o->precond, degree, check, &inf)))
+    if ((rc = pcg_fcg_mixed(h, L, U, p, q, r, r32, r32 + nl, o->rtol, o->maxiter, o->precond,
+                            degree, check, &inf)))
       return rc;
   } else if (o->method == 1) {
     float* p32 = (float*)p;

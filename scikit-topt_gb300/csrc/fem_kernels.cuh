@@ -123,7 +123,8 @@ __global__ void k_fix_zero_diag(SellT sp, T* __restrict__ vals) {
   }
 }
 
-// Inverse of every diagonal block (block Jacobi), computed in double.
+// Inverse of every diagonal block (block Jacobi), in the precision of the
+// level (the FP32 smoother needs no FP64 arithmetic).
 template <typename T, int BS>
 __global__ void k_block_diag_inv(SellT sp, const T* __restrict__ vals, T* __restrict__ dinv) {
   TOPT_KERNEL_COUNT();
@@ -132,17 +133,17 @@ __global__ void k_block_diag_inv(SellT sp, const T* __restrict__ vals, T* __rest
     const int64_t pd = sp.diag[i];
     T* O = dinv + i * BS * BS;
     if (BS == 1) {
-      const double d = (double)vals[vidx<BS>(pd, 0)];
-      O[0] = (T)(d != 0.0 ? 1.0 / d : 0.0);
+      const T d = vals[vidx<BS>(pd, 0)];
+      O[0] = d != T(0) ? T(1) / d : T(0);
     } else {
-      double D[9];
+      T D[9];
 #pragma unroll
-      for (int v = 0; v < 9; ++v) D[v] = (double)vals[vidx<BS>(pd, v)];
-      const double a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5],
-                   g = D[6], h = D[7], k = D[8];
-      const double A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
-      const double det = a * A + b * B + c * C;
-      const double s = det != 0.0 ? 1.0 / det : 0.0;
+      for (int v = 0; v < 9; ++v) D[v] = vals[vidx<BS>(pd, v)];
+      const T a = D[0], b = D[1], c = D[2], d = D[3], e = D[4], f = D[5],
+              g = D[6], h = D[7], k = D[8];
+      const T A = e * k - f * h, B = -(d * k - f * g), C = d * h - e * g;
+      const T det = a * A + b * B + c * C;
+      const T s = det != T(0) ? T(1) / det : T(0);
       O[0] = (T)(A * s);
       O[1] = (T)(-(b * k - c * h) * s);
       O[2] = (T)((b * f - c * e) * s);
@@ -157,15 +158,57 @@ __global__ void k_block_diag_inv(SellT sp, const T* __restrict__ vals, T* __rest
 }
 
 // --------------------------------------------------------------------------
+// Chebyshev smoothing step fused into the operator that produced the
+// residual r (= the operator kernel's output y, held in registers):
+//   kind 1:  dn = c2 Dinv r                         (first step; x untouched)
+//   kind 2:  dn = c1 do + c2 Dinv r,  x += dn (+ do when add_old)
+// dn and do are distinct buffers (neighbouring rows still read do).
+template <typename T>
+struct ChebEp {
+  const T* dinv = nullptr;
+  const T* dold = nullptr;
+  T* dnew = nullptr;
+  T* x = nullptr;
+  T c1 = T(0), c2 = T(0);
+  int kind = 0, add_old = 0;
+};
+
+template <typename T, int BS, int L>
+__device__ __forceinline__ void cheb_epilogue(const ChebEp<T>& ep, int64_t row, const T* r) {
+  const T* D = ep.dinv + row * BS * BS;
+  T Dv[BS * BS];
+#pragma unroll
+  for (int q = 0; q < BS * BS; ++q) Dv[q] = D[q];
+#pragma unroll
+  for (int c = 0; c < BS; ++c)
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      T s = T(0);
+#pragma unroll
+      for (int d = 0; d < BS; ++d) s += Dv[c * BS + d] * r[d * L + j];
+      const int64_t idx = row * BS * L + c * L + j;
+      if (ep.kind == 1) {
+        ep.dnew[idx] = ep.c2 * s;
+      } else {
+        const T dold = ep.dold[idx];
+        const T dn = ep.c1 * dold + ep.c2 * s;
+        ep.dnew[idx] = dn;
+        ep.x[idx] += ep.add_old ? dn + dold : dn;
+      }
+    }
+}
+
+// --------------------------------------------------------------------------
 // SELL-32 BSR SpMV / SpMM: one thread per block row, no cross-lane
 // reduction; every plane load of a warp is one coalesced 32-wide access.
 // MODE 0: y = A x;  MODE 1: y = b - A x;  MODE 2: y = y - A x.
 // DOT: also reduce sum_j (x_row . y_row) per load into dot_out (fused p.Ap).
+// ep: optional Chebyshev step on the output (ep.kind 0 = none).
 template <typename T, int BS, int L, int MODE, bool DOT>
 __global__ void __launch_bounds__(256)
 k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
             const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
-            double* dot_out) {
+            double* dot_out, ChebEp<T> ep) {
   TOPT_KERNEL_COUNT();
   double dacc[L];
 #pragma unroll
@@ -204,8 +247,10 @@ k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
         else if (MODE == 1) out = b[idx] - acc[i];
         else out = y[idx] - acc[i];
         y[idx] = out;
+        acc[i] = out;
         if (DOT) dacc[i % L] += (double)x[idx] * (double)out;
       }
+      if (ep.kind) cheb_epilogue<T, BS, L>(ep, row, acc);
     }
   }
   if (DOT) {
@@ -232,7 +277,7 @@ __global__ void __launch_bounds__(256)
 k_mf_apply(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
            const uint8_t* __restrict__ mask, const T* __restrict__ x,
            const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
-           double* dot_out) {
+           double* dot_out, ChebEp<T> ep) {
   TOPT_KERNEL_COUNT();
   __shared__ T Ks[24 * 24];
   for (int i = threadIdx.x; i < 576; i += blockDim.x) Ks[i] = K0[i];
@@ -293,9 +338,11 @@ k_mf_apply(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
         else if (MODE == 1) out = b[idx] - ax;
         else out = y[idx] - ax;
         y[idx] = out;
+        acc[c * L + j] = out;
         if (DOT) dacc[j] += (double)x[idx] * (double)out;
       }
     }
+    if (ep.kind) cheb_epilogue<T, 3, L>(ep, a, acc);
   }
   if (DOT) {
     __shared__ double sh[32 * L];
@@ -304,67 +351,96 @@ k_mf_apply(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
   }
 }
 
-// Single-load variant tuned for throughput: the unit matrix sits in constant
-// memory and every loop index is a compile-time constant, so each of the 576
-// FMAs per node reads its K0 operand straight from the constant bank (no
-// shared-memory load instructions); the x of the 3x3x3 node neighbourhood is
-// loaded once into registers.  nmask packs the fixed flags of a node's three
-// DOFs in bits 0-2.
+// Single-load operator: the unit matrix sits in constant memory and every
+// loop index is a compile-time constant, so each of the 576 FMAs per node
+// reads its K0 operand straight from the constant bank.  nmask packs the
+// fixed flags of a node's three DOFs in bits 0-2; hoff(a, d) is the offset of
+// local node a along axis d (MeshHex order).
 __constant__ float c_K0f[576];
 
 __host__ __device__ constexpr int hoff(int a, int d) {
   return d == 0 ? (0xD4 >> a) & 1 : (d == 1 ? (0xB2 >> a) & 1 : (0xE8 >> a) & 1);
 }
 
+// Tiled variant: a CTA owns a kMfTY x kMfTX x kMfTZ block of nodes (y
+// fastest, one node per thread).  It stages the node halo (x as float4 per
+// node, fixed DOFs and nodes outside the grid zeroed) and the coefficients of
+// every cell touching the tile (0 outside the grid) in shared memory with
+// coalesced loads, so the per-node work is branch-free: per cell, 8 LDS.128
+// of its nodes and 72 FFMA with constant-bank K0 operands.  Two CTAs per SM
+// overlap one tile's staging with the other's arithmetic.
+constexpr int kMfTY = 32, kMfTX = 4, kMfTZ = 2;
+constexpr int kMfThreads = kMfTY * kMfTX * kMfTZ;
+constexpr int kMfHY = kMfTY + 2, kMfHX = kMfTX + 2, kMfHZ = kMfTZ + 2;
+constexpr int kMfCY = kMfTY + 1, kMfCX = kMfTX + 1, kMfCZ = kMfTZ + 1;
+
+inline int64_t mf_tiles(const MfGrid& g) {
+  return (int64_t)((g.ny + kMfTY) / kMfTY) * ((g.nx + kMfTX) / kMfTX) *
+         ((g.nz + kMfTZ) / kMfTZ);
+}
+
 template <int MODE, bool DOT>
-__global__ void __launch_bounds__(128)
-k_mf_apply1(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ nmask,
-            const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
-            double* partials, unsigned* counter, double* dot_out) {
+__global__ void __launch_bounds__(kMfThreads, 2)
+k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ nmask,
+          const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
+          double* partials, unsigned* counter, double* dot_out, ChebEp<float> ep) {
   TOPT_KERNEL_COUNT();
+  __shared__ float4 xs[kMfHZ][kMfHX][kMfHY];
+  __shared__ float cs[kMfCZ][kMfCX][kMfCY];
   const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
-  const int nn = nx1 * ny1 * nz1;
-  double dacc[1] = {0.0};
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nn; a += gridDim.x * blockDim.x) {
-    const int iy = a % ny1;
-    const int ix = (a / ny1) % nx1;
-    const int iz = a / (ny1 * nx1);
-    float xn[27][3];
-#pragma unroll
-    for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-      for (int dx = -1; dx <= 1; ++dx)
-#pragma unroll
-        for (int dy = -1; dy <= 1; ++dy) {
-          const int k = (dz + 1) * 9 + (dx + 1) * 3 + (dy + 1);
-          const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
-          const bool in = jx >= 0 && jy >= 0 && jz >= 0 && jx < nx1 && jy < ny1 && jz < nz1;
-          const int nb = jy + ny1 * (jx + nx1 * jz);
-          const int m = in ? (nmask ? nmask[nb] : 0) : 7;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) xn[k][c] = ((m >> c) & 1) ? 0.0f : x[nb * 3 + c];
-        }
-    float acc[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-    for (int la = 0; la < 8; ++la) {
-      const int cx = ix - hoff(la, 0), cy = iy - hoff(la, 1), cz = iz - hoff(la, 2);
-      const bool in = cx >= 0 && cy >= 0 && cz >= 0 && cx < g.nx && cy < g.ny && cz < g.nz;
-      const float s = in ? coef[cy + g.ny * (cx + g.nx * cz)] : 0.0f;
-      float part[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-      for (int lb = 0; lb < 8; ++lb) {
-        const int k = (hoff(lb, 2) - hoff(la, 2) + 1) * 9 + (hoff(lb, 0) - hoff(la, 0) + 1) * 3 +
-                      (hoff(lb, 1) - hoff(la, 1) + 1);
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-#pragma unroll
-          for (int d = 0; d < 3; ++d)
-            part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xn[k][d], part[c]);
-      }
-#pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
+  // 1-D grid of tiles, y tiles fastest (the block index is linear for the
+  // deterministic grid reduction)
+  const int nty = (ny1 + kMfTY - 1) / kMfTY, ntx = (nx1 + kMfTX - 1) / kMfTX;
+  const int bt = blockIdx.x;
+  const int ty = (bt % nty) * kMfTY, tx = ((bt / nty) % ntx) * kMfTX,
+            tz = (bt / (nty * ntx)) * kMfTZ;
+  for (int i = threadIdx.x; i < kMfHZ * kMfHX * kMfHY; i += kMfThreads) {
+    const int hy = i % kMfHY, hx = (i / kMfHY) % kMfHX, hz = i / (kMfHY * kMfHX);
+    const int jy = ty - 1 + hy, jx = tx - 1 + hx, jz = tz - 1 + hz;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (jy >= 0 && jx >= 0 && jz >= 0 && jy < ny1 && jx < nx1 && jz < nz1) {
+      const int nb = jy + ny1 * (jx + nx1 * jz);
+      const int m = nmask ? nmask[nb] : 0;
+      v.x = (m & 1) ? 0.f : x[nb * 3 + 0];
+      v.y = (m & 2) ? 0.f : x[nb * 3 + 1];
+      v.z = (m & 4) ? 0.f : x[nb * 3 + 2];
     }
+    xs[hz][hx][hy] = v;
+  }
+  for (int i = threadIdx.x; i < kMfCZ * kMfCX * kMfCY; i += kMfThreads) {
+    const int cy = i % kMfCY, cx = (i / kMfCY) % kMfCX, cz = i / (kMfCY * kMfCX);
+    const int ey = ty - 1 + cy, ex = tx - 1 + cx, ez = tz - 1 + cz;
+    const bool in = ey >= 0 && ex >= 0 && ez >= 0 && ey < g.ny && ex < g.nx && ez < g.nz;
+    cs[cz][cx][cy] = in ? coef[ey + g.ny * (ex + g.nx * ez)] : 0.f;
+  }
+  __syncthreads();
+  const int ly = threadIdx.x % kMfTY, lx = (threadIdx.x / kMfTY) % kMfTX,
+            lz = threadIdx.x / (kMfTY * kMfTX);
+  float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int la = 0; la < 8; ++la) {
+    float part[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int lb = 0; lb < 8; ++lb) {
+      const float4 v = xs[lz + 1 - hoff(la, 2) + hoff(lb, 2)][lx + 1 - hoff(la, 0) + hoff(lb, 0)]
+                         [ly + 1 - hoff(la, 1) + hoff(lb, 1)];
+      const float xv[3] = {v.x, v.y, v.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
+    }
+    const float s = cs[lz + 1 - hoff(la, 2)][lx + 1 - hoff(la, 0)][ly + 1 - hoff(la, 1)];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
+  }
+  const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
+  double dacc[1] = {0.0};
+  if (iy < ny1 && ix < nx1 && iz < nz1) {
+    const int a = iy + ny1 * (ix + nx1 * iz);
     const int ma = nmask ? nmask[a] : 0;
+    // fixed rows act as identity rows (the staged x of a fixed DOF is 0)
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const int64_t idx = (int64_t)a * 3 + c;
@@ -374,8 +450,10 @@ k_mf_apply1(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict_
       else if (MODE == 1) out = b[idx] - ax;
       else out = y[idx] - ax;
       y[idx] = out;
+      acc[c] = out;
       if (DOT) dacc[0] += (double)x[idx] * (double)out;
     }
+    if (ep.kind) cheb_epilogue<float, 3, 1>(ep, a, acc);
   }
   if (DOT) {
     __shared__ double sh[32];
@@ -384,7 +462,8 @@ k_mf_apply1(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict_
   }
 }
 
-// Inverted 3x3 diagonal blocks of the matrix-free operator (block Jacobi):
+// Inverted 3x3 diagonal blocks of the matrix-free operator (block Jacobi, in
+// the operator's precision):
 // D_a = sum_c coef_c K0[la, la], fixed DOFs as identity rows / columns.
 template <typename T>
 __global__ void k_mf_diag_inv(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
@@ -398,34 +477,34 @@ __global__ void k_mf_diag_inv(MfGrid g, const T* __restrict__ K0, const T* __res
     const int iy = ai % ny1;
     const int ix = (ai / ny1) % nx1;
     const int iz = ai / (ny1 * nx1);
-    double D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    T D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     for (int la = 0; la < 8; ++la) {
       const int cx = ix - c_hex_off[la][0], cy = iy - c_hex_off[la][1],
                 cz = iz - c_hex_off[la][2];
       if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
-      const double s = (double)coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
+      const T s = coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
       for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d) D[c * 3 + d] += s * (double)K0[(3 * la + c) * 24 + 3 * la + d];
+        for (int d = 0; d < 3; ++d) D[c * 3 + d] += s * K0[(3 * la + c) * 24 + 3 * la + d];
     }
     if (mask) {
       for (int c = 0; c < 3; ++c)
         for (int d = 0; d < 3; ++d)
-          if (mask[a * 3 + c] || mask[a * 3 + d]) D[c * 3 + d] = (c == d) ? 1.0 : 0.0;
+          if (mask[a * 3 + c] || mask[a * 3 + d]) D[c * 3 + d] = (c == d) ? T(1) : T(0);
     }
-    const double A = D[4] * D[8] - D[5] * D[7], B = -(D[3] * D[8] - D[5] * D[6]),
-                 C = D[3] * D[7] - D[4] * D[6];
-    const double det = D[0] * A + D[1] * B + D[2] * C;
-    const double si = det != 0.0 ? 1.0 / det : 0.0;
+    const T A = D[4] * D[8] - D[5] * D[7], B = -(D[3] * D[8] - D[5] * D[6]),
+            C = D[3] * D[7] - D[4] * D[6];
+    const T det = D[0] * A + D[1] * B + D[2] * C;
+    const T si = det != T(0) ? T(1) / det : T(0);
     T* O = dinv + a * 9;
-    O[0] = (T)(A * si);
-    O[1] = (T)(-(D[1] * D[8] - D[2] * D[7]) * si);
-    O[2] = (T)((D[1] * D[5] - D[2] * D[4]) * si);
-    O[3] = (T)(B * si);
-    O[4] = (T)((D[0] * D[8] - D[2] * D[6]) * si);
-    O[5] = (T)(-(D[0] * D[5] - D[2] * D[3]) * si);
-    O[6] = (T)(C * si);
-    O[7] = (T)(-(D[0] * D[7] - D[1] * D[6]) * si);
-    O[8] = (T)((D[0] * D[4] - D[1] * D[3]) * si);
+    O[0] = A * si;
+    O[1] = -(D[1] * D[8] - D[2] * D[7]) * si;
+    O[2] = (D[1] * D[5] - D[2] * D[4]) * si;
+    O[3] = B * si;
+    O[4] = (D[0] * D[8] - D[2] * D[6]) * si;
+    O[5] = -(D[0] * D[5] - D[2] * D[3]) * si;
+    O[6] = C * si;
+    O[7] = -(D[0] * D[7] - D[1] * D[6]) * si;
+    O[8] = (D[0] * D[4] - D[1] * D[3]) * si;
   }
 }
 
@@ -436,7 +515,7 @@ template <typename T, int BS, int L, int MODE, bool DOT>
 __global__ void __launch_bounds__(256)
 k_sell_spmv_warp(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
                  const T* __restrict__ b, T* __restrict__ y, double* partials,
-                 unsigned* counter, double* dot_out) {
+                 unsigned* counter, double* dot_out, ChebEp<T> ep) {
   TOPT_KERNEL_COUNT();
   const int lane = threadIdx.x & 31;
   const int64_t w0 = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -476,11 +555,101 @@ k_sell_spmv_warp(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
         else if (MODE == 1) out = b[idx] - acc[q];
         else out = y[idx] - acc[q];
         y[idx] = out;
+        acc[q] = out;
         if (DOT) dacc[q % L] += (double)x[idx] * (double)out;
       }
+      if (ep.kind) cheb_epilogue<T, BS, L>(ep, row, acc);
     }
   }
   if (DOT) {
+    __shared__ double sh[32 * L];
+    block_sum<double, L>(dacc, sh);
+    grid_finish<double, L>(dacc, partials, counter, dot_out);
+  }
+}
+
+// Mid-size levels (3x3 blocks): three threads per block row, one per output
+// component, so a level of a few ten thousand rows still fills the GPU.  A
+// CTA of 192 threads covers two slices; warp (slice, c) reads plane row c of
+// every block with 32-wide coalesced loads.  The Chebyshev epilogue needs the
+// three residual components of a row: they meet in shared memory.
+template <typename T, int L, int MODE, bool DOT>
+__global__ void __launch_bounds__(192)
+k_sell_spmv3(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
+             const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
+             double* dot_out, ChebEp<T> ep) {
+  TOPT_KERNEL_COUNT();
+  __shared__ T rs[2][3][32 * L];
+  const int sl = threadIdx.x / 96, c = (threadIdx.x % 96) >> 5, lane = threadIdx.x & 31;
+  const int64_t nsl = (sp.nrows + 31) >> 5;
+  T tacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) tacc[j] = T(0);
+  for (int64_t s0 = 2 * (int64_t)blockIdx.x; s0 < nsl; s0 += 2 * (int64_t)gridDim.x) {
+    const int64_t slice = s0 + sl;
+    const int64_t row = slice * 32 + lane;
+    const bool valid = slice < nsl && row < sp.nrows;
+    T acc[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) acc[j] = T(0);
+    if (slice < nsl) {
+      const int64_t g0 = sp.grp_of_slice[slice], g1 = sp.grp_of_slice[slice + 1];
+#pragma unroll 3
+      for (int64_t g = g0; g < g1; ++g) {
+        const int64_t col = sp.col[g * 32 + lane];
+        const T* V = vals + g * (9 * 32) + lane;
+        const T a0 = V[(c * 3 + 0) * 32], a1 = V[(c * 3 + 1) * 32], a2 = V[(c * 3 + 2) * 32];
+#pragma unroll
+        for (int j = 0; j < L; ++j)
+          acc[j] += a0 * x[(col * 3 + 0) * L + j] + a1 * x[(col * 3 + 1) * L + j] +
+                    a2 * x[(col * 3 + 2) * L + j];
+      }
+    }
+    T out[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) out[j] = T(0);
+    if (valid) {
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int64_t idx = (row * 3 + c) * L + j;
+        if (MODE == 0) out[j] = acc[j];
+        else if (MODE == 1) out[j] = b[idx] - acc[j];
+        else out[j] = y[idx] - acc[j];
+        y[idx] = out[j];
+        if (DOT) tacc[j] += x[idx] * out[j];
+      }
+    }
+    if (ep.kind) {   // uniform over the grid: the barriers below are safe
+#pragma unroll
+      for (int j = 0; j < L; ++j) rs[sl][c][lane * L + j] = out[j];
+      __syncthreads();
+      if (valid) {
+        const T* D = ep.dinv + row * 9 + c * 3;
+        const T D0 = D[0], D1 = D[1], D2 = D[2];
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+          T s = T(0);
+          s += D0 * rs[sl][0][lane * L + j];
+          s += D1 * rs[sl][1][lane * L + j];
+          s += D2 * rs[sl][2][lane * L + j];
+          const int64_t idx = (row * 3 + c) * L + j;
+          if (ep.kind == 1) {
+            ep.dnew[idx] = ep.c2 * s;
+          } else {
+            const T dold = ep.dold[idx];
+            const T dn = ep.c1 * dold + ep.c2 * s;
+            ep.dnew[idx] = dn;
+            ep.x[idx] += ep.add_old ? dn + dold : dn;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (DOT) {
+    double dacc[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) dacc[j] = (double)tacc[j];
     __shared__ double sh[32 * L];
     block_sum<double, L>(dacc, sh);
     grid_finish<double, L>(dacc, partials, counter, dot_out);
@@ -509,9 +678,9 @@ __global__ void k_block_jacobi(int64_t n_nodes, const T* __restrict__ dinv,
                                const T* __restrict__ r, T* __restrict__ z,
                                double* partials, unsigned* counter, double* dot_out) {
   TOPT_KERNEL_COUNT();
-  double dacc[L];
+  T tacc[L];
 #pragma unroll
-  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  for (int j = 0; j < L; ++j) tacc[j] = T(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
        i += (int64_t)gridDim.x * blockDim.x) {
     const T* D = dinv + i * BS * BS;
@@ -526,10 +695,13 @@ __global__ void k_block_jacobi(int64_t n_nodes, const T* __restrict__ dinv,
 #pragma unroll
         for (int d = 0; d < BS; ++d) s += D[c * BS + d] * rv[d * L + j];
         z[i * BS * L + c * L + j] = s;
-        if (DOT) dacc[j] += (double)s * (double)rv[c * L + j];
+        if (DOT) tacc[j] += s * rv[c * L + j];
       }
   }
   if (DOT) {
+    double dacc[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) dacc[j] = (double)tacc[j];
     __shared__ double sh[32 * L];
     block_sum<double, L>(dacc, sh);
     grid_finish<double, L>(dacc, partials, counter, dot_out);
@@ -541,27 +713,31 @@ template <typename T, int L>
 __global__ void k_dot(int64_t n, const T* __restrict__ x, const T* __restrict__ y,
                       double* partials, unsigned* counter, double* out) {
   TOPT_KERNEL_COUNT();
-  double acc[L];
+  // per-thread sums in T (FP64 arithmetic is scarce on this part), then FP64
+  T tacc[L];
 #pragma unroll
-  for (int j = 0; j < L; ++j) acc[j] = 0.0;
+  for (int j = 0; j < L; ++j) tacc[j] = T(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int j = 0; j < L; ++j) acc[j] += (double)x[i * L + j] * (double)y[i * L + j];
+    for (int j = 0; j < L; ++j) tacc[j] += x[i * L + j] * y[i * L + j];
   }
+  double acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = (double)tacc[j];
   __shared__ double sh[32 * L];
   block_sum<double, L>(acc, sh);
   grid_finish<double, L>(acc, partials, counter, out);
 }
 
 // PCG update: alpha_j = rz_j / pq_j (0 when frozen or pq <= 0);
-// x += alpha p; r -= alpha q; partial sums of r.r.
+// x += alpha p; r -= alpha q; partial sums of r.r; r32 (optional) = float(r).
 template <typename T, int L>
 __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
                              const double* __restrict__ pq, const int* __restrict__ active,
                              const T* __restrict__ p, const T* __restrict__ q,
                              T* __restrict__ x, T* __restrict__ r, double* partials,
-                             unsigned* counter, double* rr_out) {
+                             unsigned* counter, double* rr_out, float* __restrict__ r32) {
   TOPT_KERNEL_COUNT();
   T alpha[L];
 #pragma unroll
@@ -580,6 +756,7 @@ __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
       x[q_] += alpha[j] * p[q_];
       const T rv = r[q_] - alpha[j] * q[q_];
       r[q_] = rv;
+      if (r32) r32[q_] = (float)rv;
       acc[j] += (double)rv * (double)rv;
     }
   }
@@ -589,9 +766,9 @@ __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
 }
 
 // Two dots sharing z: out[0..L) = r.z, out[L..2L) = q.z (flexible CG).
-template <typename T, int L>
+template <typename T, typename TZ, int L>
 __global__ void k_dot2(int64_t n, const T* __restrict__ r, const T* __restrict__ q,
-                       const T* __restrict__ z, double* partials, unsigned* counter,
+                       const TZ* __restrict__ z, double* partials, unsigned* counter,
                        double* out) {
   TOPT_KERNEL_COUNT();
   double acc[2 * L];
@@ -613,10 +790,10 @@ __global__ void k_dot2(int64_t n, const T* __restrict__ r, const T* __restrict__
 
 // Flexible (Polak-Ribiere) direction: beta_j = -alpha_j (q.z_new)_j / rz_old_j
 // with alpha_j = rz_old_j / pq_j, i.e. beta = -(q.z_new) / pq; p = z + beta p.
-template <typename T, int L>
+template <typename T, typename TZ, int L>
 __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
                                 const double* __restrict__ pq, const int* __restrict__ active,
-                                const T* __restrict__ z, T* __restrict__ p) {
+                                const TZ* __restrict__ z, T* __restrict__ p) {
   TOPT_KERNEL_COUNT();
   T beta[L];
 #pragma unroll
@@ -625,15 +802,15 @@ __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int j = 0; j < L; ++j) p[i * L + j] = z[i * L + j] + beta[j] * p[i * L + j];
+    for (int j = 0; j < L; ++j) p[i * L + j] = (T)z[i * L + j] + beta[j] * p[i * L + j];
   }
 }
 
 // p = z + beta p with beta_j = rz_new_j / rz_old_j (p = z on the first step).
-template <typename T, int L>
+template <typename T, typename TZ, int L>
 __global__ void k_pcg_direction(int64_t n, const double* __restrict__ rz_new,
                                 const double* __restrict__ rz_old, int first,
-                                const T* __restrict__ z, T* __restrict__ p) {
+                                const TZ* __restrict__ z, T* __restrict__ p) {
   TOPT_KERNEL_COUNT();
   T beta[L];
 #pragma unroll
@@ -643,7 +820,7 @@ __global__ void k_pcg_direction(int64_t n, const double* __restrict__ rz_new,
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int j = 0; j < L; ++j)   // p = z exactly on the first step (p may hold garbage)
-      p[i * L + j] = first ? z[i * L + j] : z[i * L + j] + beta[j] * p[i * L + j];
+      p[i * L + j] = first ? (T)z[i * L + j] : (T)z[i * L + j] + beta[j] * p[i * L + j];
   }
 }
 
@@ -691,6 +868,22 @@ __global__ void k_fill(int64_t n, T v, T* __restrict__ a) {
        i += (int64_t)gridDim.x * blockDim.x)
     a[i] = v;
 }
+// y += a x
+template <typename T>
+__global__ void k_axpy(int64_t n, T a, const T* __restrict__ x, T* __restrict__ y) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] += a * x[i];
+}
+// y = a x
+template <typename T>
+__global__ void k_scale(int64_t n, T a, const T* __restrict__ x, T* __restrict__ y) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = a * x[i];
+}
 // U += double(d)
 __global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
                                  double* __restrict__ u) {
@@ -731,16 +924,20 @@ struct GridT {
   int ncx, ncy, ncz;  // coarse cells
   const int32_t *cmx, *cmy, *cmz;
   const int32_t *c0x, *c0y, *c0z;
-  const double *w1x, *w1y, *w1z;
+  const float *w1x, *w1y, *w1z;   // 0, 1/2 or 1: exact in FP32
   // restriction: per coarse index, first fine index and 3 weights
   const int32_t *r0x, *r0y, *r0z;
   const float *rwx, *rwy, *rwz;
 };
 
-// bc = P^T r  (coarse node gathers its <= 3x3x3 fine support, fixed order)
+// bc = P^T r  (coarse node gathers its <= 3x3x3 fine support, fixed order).
+// With dinv_c set, also the first Chebyshev step of the coarse level from a
+// zero guess: d_c = x_c = c2 Dinv_c bc.
 template <typename T, int BS, int L>
 __global__ void k_restrict(GridT g, const uint8_t* __restrict__ mask,
-                           const T* __restrict__ rf, T* __restrict__ bc) {
+                           const T* __restrict__ rf, T* __restrict__ bc,
+                           const T* __restrict__ dinv_c, T* __restrict__ d_c,
+                           T* __restrict__ x_c, T c2) {
   TOPT_KERNEL_COUNT();
   const int nnx = g.ncx + 1, nny = g.ncy + 1;
   const int nc = nnx * nny * (g.ncz + 1);
@@ -778,6 +975,20 @@ __global__ void k_restrict(GridT g, const uint8_t* __restrict__ mask,
     }
 #pragma unroll
     for (int q = 0; q < BS * L; ++q) bc[(int64_t)I * BS * L + q] = acc[q];
+    if (dinv_c) {
+      const T* D = dinv_c + (int64_t)I * BS * BS;
+#pragma unroll
+      for (int c = 0; c < BS; ++c)
+#pragma unroll
+        for (int j = 0; j < L; ++j) {
+          T s = T(0);
+#pragma unroll
+          for (int d = 0; d < BS; ++d) s += D[c * BS + d] * acc[d * L + j];
+          const int64_t idx = (int64_t)I * BS * L + c * L + j;
+          d_c[idx] = c2 * s;
+          x_c[idx] = c2 * s;
+        }
+    }
   }
 }
 
@@ -796,22 +1007,22 @@ __global__ void k_prolong_add(GridT g, const uint8_t* __restrict__ mask,
     const int fx = (F32 / fny) % fnx;
     const int fz = F32 / (fny * fnx);
     const int cx = g.c0x[fx], cy = g.c0y[fy], cz = g.c0z[fz];
-    const double ax = g.w1x[fx], ay = g.w1y[fy], az = g.w1z[fz];
+    const float ax = g.w1x[fx], ay = g.w1y[fy], az = g.w1z[fz];
     T acc[BS * L];
 #pragma unroll
     for (int q = 0; q < BS * L; ++q) acc[q] = T(0);
 #pragma unroll
     for (int oz = 0; oz < 2; ++oz) {
-      const double wz = oz ? az : 1.0 - az;
-      if (wz == 0.0) continue;
+      const float wz = oz ? az : 1.0f - az;
+      if (wz == 0.0f) continue;
 #pragma unroll
       for (int ox = 0; ox < 2; ++ox) {
-        const double wx = (ox ? ax : 1.0 - ax) * wz;
-        if (wx == 0.0) continue;
+        const float wx = (ox ? ax : 1.0f - ax) * wz;
+        if (wx == 0.0f) continue;
 #pragma unroll
         for (int oy = 0; oy < 2; ++oy) {
-          const double wd = (oy ? ay : 1.0 - ay) * wx;
-          if (wd == 0.0) continue;
+          const float wd = (oy ? ay : 1.0f - ay) * wx;
+          if (wd == 0.0f) continue;
           const T w = (T)wd;
           const int64_t cn = (cy + oy) + cny * ((cx + ox) + cnx * (int64_t)(cz + oz));
 #pragma unroll
@@ -884,12 +1095,13 @@ k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
             const int64_t n = t[(int64_t)a * n_elem_f + e];
             const int iy = (int)(n % fny), ix = (int)((n / fny) % fnx),
                       iz = (int)(n / (fny * fnx));
-            const double xi = (double)(ix - ax0) / (double)(ax1 - ax0);
-            const double yi = (double)(iy - ay0) / (double)(ay1 - ay0);
-            const double zi = (double)(iz - az0) / (double)(az1 - az0);
-            const double w = (c_hex_off[k][0] ? xi : 1.0 - xi) *
-                             (c_hex_off[k][1] ? yi : 1.0 - yi) *
-                             (c_hex_off[k][2] ? zi : 1.0 - zi);
+            // 0, 1/2 or 1 per axis: exact in FP32 (FP64 arithmetic is scarce)
+            const float xi = (float)(ix - ax0) / (float)(ax1 - ax0);
+            const float yi = (float)(iy - ay0) / (float)(ay1 - ay0);
+            const float zi = (float)(iz - az0) / (float)(az1 - az0);
+            const float w = (c_hex_off[k][0] ? xi : 1.0f - xi) *
+                            (c_hex_off[k][1] ? yi : 1.0f - yi) *
+                            (c_hex_off[k][2] ? zi : 1.0f - zi);
             Wm[a * 8 + k] = (T)w;
           }
           if (threadIdx.x < NF) {

@@ -12,7 +12,8 @@ static const int kFB = 256;
 // Device-resident state of an OC bisection (oc.py:16-95).
 struct OcState {
   double l1, l2, lmid, vol_error;
-  int it, done, steps, pad;
+  int it, done, steps;
+  int need64;   // the FP32 volume of this step was too close to a decision edge
 };
 
 }  // namespace topt
@@ -33,4 +34,6 @@ struct topt_filter {
   int64_t n_nondesign = 0;
   // OC work
   topt::DevBuf cand, state, partials, counter, rho_e, rho_new;
+  // FP32 bracketing of the bisection: W in FP32 and per-step inputs
+  topt::DevBuf vals32, cand32, oc32;
 };

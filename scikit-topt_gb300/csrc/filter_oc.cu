@@ -199,14 +199,46 @@ __device__ __forceinline__ double clip_nan(double a, double lo, double hi) {
   return (a > hi) ? hi : a;
 }
 
+__global__ void k_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
+}
+
+// Bisection step gates: 0 = every step until done, 1 = only steps whose FP32
+// volume was ambiguous (need64), 2 = unconditionally (final pass).
+__device__ __forceinline__ bool oc_gate(const OcState* st, int mode) {
+  if (mode == 2) return true;
+  if (st->done) return false;
+  return mode == 0 || st->need64;
+}
+
+// One decision of the bisection (oc.py:16-95): stop when the volume error is
+// within vol_tol, the iteration cap is reached or the bracket is narrower
+// than tolerance; otherwise halve the bracket towards the error's sign.
+__device__ __forceinline__ void oc_decide(OcState* st, const topt_oc_params& prm, double ve) {
+  st->steps = st->it + 1;
+  st->need64 = 0;
+  if (fabs(ve) < prm.vol_tol || st->it >= prm.max_iter ||
+      fabs(st->l2 - st->l1) <= prm.tolerance) {
+    st->done = 1;
+  } else {
+    if (ve > 0) st->l1 = st->lmid;
+    else st->l2 = st->lmid;
+    st->it += 1;
+    st->lmid = 0.5 * (st->l1 + st->l2);
+  }
+}
+
 __global__ void k_oc_candidate(int64_t nd, const int32_t* __restrict__ design,
                                const double* __restrict__ dc, double dc_scale,
                                const double* __restrict__ rho_e,
                                const OcState* __restrict__ st, topt_oc_params prm,
                                double* __restrict__ cand, double* __restrict__ rho_new,
-                               double* __restrict__ scaling) {
+                               double* __restrict__ scaling, int mode) {
   TOPT_KERNEL_COUNT();
-  if (st->done) return;
+  if (!oc_gate(st, mode)) return;
   const double lm = st->lmid;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -303,9 +335,9 @@ __global__ void k_oc_volume(int64_t nd, const int32_t* __restrict__ rowptr,
                             const int32_t* __restrict__ col, const double* __restrict__ w,
                             const double* __restrict__ cand, const double* __restrict__ vol,
                             double vol_sum, topt_oc_params prm, double tbe, double den,
-                            OcState* st, double* partials, unsigned* counter) {
+                            OcState* st, double* partials, unsigned* counter, int mode) {
   TOPT_KERNEL_COUNT();
-  if (st->done) return;
+  if (!oc_gate(st, mode)) return;
   double acc[1] = {0.0};
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -322,15 +354,96 @@ __global__ void k_oc_volume(int64_t nd, const int32_t* __restrict__ rowptr,
     if (threadIdx.x == 0) {
       const double ve = total / vol_sum - prm.vol_frac;
       st->vol_error = ve;
-      st->steps = st->it + 1;
-      if (fabs(ve) < prm.vol_tol || st->it >= prm.max_iter ||
-          fabs(st->l2 - st->l1) <= prm.tolerance) {
-        st->done = 1;
+      if (mode != 2) oc_decide(st, prm, ve);
+    }
+  }
+}
+
+// FP32 bracketing of the bisection.  Per call: the sensitivity part of the
+// scaling rate (-dc/scale)^eta, rho and the move-limit box in FP32.  Per
+// step: the candidate and the filtered, projected volume in FP32, and the
+// decision taken from it only when it is unambiguous: the FP32 volume error
+// lies within err of the FP64 one (err bounds the FP32 rounding through the
+// filter and the projection slope), so the decision of the FP64 bisection --
+// the sign of the error and |error| < vol_tol -- is the same whenever
+// |ve32| > err and ||ve32| - vol_tol| > err.  Otherwise need64 is set and
+// the FP64 kernels evaluate that step exactly.  The path of lmid values, and
+// hence the result, is that of the FP64 bisection.
+struct Oc32 {
+  float sq, r, lo, hi;
+};
+
+__global__ void k_oc_prep32(int64_t nd, const int32_t* __restrict__ design,
+                            const double* __restrict__ dc, double dc_scale,
+                            const double* __restrict__ rho_e, topt_oc_params prm,
+                            Oc32* __restrict__ out) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double q = -(dc[design[i]] / dc_scale);
+    const double sq = (prm.eta == 0.5) ? sqrt(q) : pow(q, prm.eta);
+    const double r = rho_e[i];
+    Oc32 o;
+    o.sq = (float)sq;
+    o.r = (float)r;
+    o.lo = (float)fmax(r - prm.move_limit, prm.rho_min);
+    o.hi = (float)fmin(r + prm.move_limit, prm.rho_max);
+    out[i] = o;
+  }
+}
+
+__device__ __forceinline__ float clipf_nan(float a, float lo, float hi) {
+  a = (a < lo) ? lo : a;
+  return (a > hi) ? hi : a;
+}
+
+__global__ void k_oc_cand32(int64_t nd, const int32_t* __restrict__ design,
+                            const Oc32* __restrict__ in, const OcState* __restrict__ st,
+                            topt_oc_params prm, float* __restrict__ cand) {
+  TOPT_KERNEL_COUNT();
+  if (st->done) return;
+  __shared__ float s_lam;
+  if (threadIdx.x == 0) s_lam = (float)pow(st->lmid + prm.eps, -prm.eta);
+  __syncthreads();
+  const float lam = s_lam, smin = (float)prm.scaling_min, smax = (float)prm.scaling_max;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const Oc32 o = in[i];
+    const float sr = clipf_nan(o.sq * lam, smin, smax);
+    cand[design[i]] = clipf_nan(o.r * sr, o.lo, o.hi);
+  }
+}
+
+__global__ void k_oc_vol32(int64_t nd, const int32_t* __restrict__ rowptr,
+                           const int32_t* __restrict__ col, const float* __restrict__ w,
+                           const float* __restrict__ cand, const double* __restrict__ vol,
+                           double vol_sum, topt_oc_params prm, float tbe, float den,
+                           double err, OcState* st, double* partials, unsigned* counter) {
+  TOPT_KERNEL_COUNT();
+  if (st->done) return;
+  const float beta = (float)prm.beta, beta_eta = (float)prm.beta_eta;
+  float tacc = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float s = 0.0f;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) s += w[k] * cand[col[k]];
+    const float hp = (tbe + tanhf((s - beta_eta) * beta)) / den;
+    tacc += hp * (float)vol[i];
+  }
+  double acc[1] = {(double)tacc};
+  __shared__ double sh[32];
+  __shared__ double total;
+  block_sum<double, 1>(acc, sh);
+  if (grid_finish<double, 1>(acc, partials, counter, &total)) {
+    if (threadIdx.x == 0) {
+      const double ve = total / vol_sum - prm.vol_frac;
+      const double a = fabs(ve);
+      if (!(a > err) || fabs(a - prm.vol_tol) <= err) {
+        st->need64 = 1;
       } else {
-        if (ve > 0) st->l1 = st->lmid;
-        else st->l2 = st->lmid;
-        st->it += 1;
-        st->lmid = 0.5 * (st->l1 + st->l2);
+        st->need64 = 0;
+        st->vol_error = ve;
+        oc_decide(st, prm, ve);
       }
     }
   }
@@ -537,14 +650,43 @@ int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rh
   const int32_t* design = f->design.as<int32_t>();
   k_gather<<<g, kFB, 0, f->stream>>>(nd, design, rho, f->rho_e.as<double>());
   OcState* st = f->state.as<OcState>();
-  for (int k = 0; k < max_steps; ++k) {
+  const bool bracket = !(prm->flags & TOPT_OC_EXACT);
+  auto fp64_step = [&](int mode) {
     k_oc_candidate<<<g, kFB, 0, f->stream>>>(nd, design, dc, dc_scale, f->rho_e.as<double>(),
                                              st, *prm, f->cand.as<double>(),
-                                             f->rho_new.as<double>(), scaling);
+                                             f->rho_new.as<double>(), scaling, mode);
     k_oc_volume<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(), f->colfull.as<int32_t>(),
                                           f->vals.as<double>(), f->cand.as<double>(), vol,
                                           vol_sum, *prm, tbe, den, st,
-                                          f->partials.as<double>(), f->counter.as<unsigned>());
+                                          f->partials.as<double>(), f->counter.as<unsigned>(),
+                                          mode);
+  };
+  if (bracket) {
+    if (!f->vals32.p) {
+      if ((rc = f->vals32.alloc(sizeof(float) * std::max<int64_t>(f->nnz, 1)))) return rc;
+      if ((rc = f->cand32.alloc(sizeof(float) * f->n_elem))) return rc;
+      if ((rc = f->oc32.alloc(sizeof(Oc32) * nd))) return rc;
+      k_to_f32<<<grid_for(f->nnz, kFB, f->sm * 8), kFB, 0, f->stream>>>(
+          f->nnz, f->vals.as<double>(), f->vals32.as<float>());
+    }
+    k_oc_prep32<<<g, kFB, 0, f->stream>>>(nd, design, dc, dc_scale, f->rho_e.as<double>(), *prm,
+                                          f->oc32.as<Oc32>());
+    // bound on |ve32 - ve64|: FP32 rounding of the candidate and the filtered
+    // density (<= 1.5e-6 absolute for weights summing to 1) amplified by the
+    // projection slope beta/den, plus the FP32 tanh and partial sums; doubled
+    const double err = 2.0 * (2.0e-6 * (1.0 + prm->beta / den) + 1.0e-6);
+    for (int k = 0; k < max_steps; ++k) {
+      k_oc_cand32<<<g, kFB, 0, f->stream>>>(nd, design, f->oc32.as<Oc32>(), st, *prm,
+                                            f->cand32.as<float>());
+      k_oc_vol32<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(), f->colfull.as<int32_t>(),
+                                           f->vals32.as<float>(), f->cand32.as<float>(), vol,
+                                           vol_sum, *prm, (float)tbe, (float)den, err, st,
+                                           f->partials.as<double>(), f->counter.as<unsigned>());
+      fp64_step(1);
+    }
+    fp64_step(2);   // exact candidate and volume error at the final lmid
+  } else {
+    for (int k = 0; k < max_steps; ++k) fp64_step(0);
   }
   k_scatter<<<g, kFB, 0, f->stream>>>(nd, design, f->rho_new.as<double>(), rho);
   TOPT_CHECK_LAUNCH("oc_bisect");

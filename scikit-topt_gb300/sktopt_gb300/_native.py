@@ -20,6 +20,7 @@ TOPT_CUDA_ERROR = 5
 TOPT_NO_MEMORY = 6
 TOPT_F64 = 0
 TOPT_F32 = 1
+TOPT_OC_EXACT = 1
 
 STATUS_NAMES = {
     TOPT_OK: "ok", TOPT_MAXITER: "max-iter", TOPT_NONFINITE: "non-finite",
@@ -67,7 +68,7 @@ class OcParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in (
         "rho_min", "rho_max", "move_limit", "eta", "eps", "vol_frac", "beta",
         "beta_eta", "scaling_min", "scaling_max", "vol_tol", "l1", "l2",
-        "tolerance")] + [("max_iter", C.c_int32), ("pad", C.c_int32)]
+        "tolerance")] + [("max_iter", C.c_int32), ("flags", C.c_int32)]
 
 
 _P = C.c_void_p

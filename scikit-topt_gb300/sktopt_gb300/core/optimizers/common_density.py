@@ -96,6 +96,9 @@ class DensityMethodConfig:
     precond: Literal["mg", "jacobi", "auto"] = "auto"
     solver_rtol: float = 1e-8
     inner_rtol: float = 1e-4
+    # OC bisection: FP32 evaluation of each step, FP64 only near a decision
+    # edge (same result as the all-FP64 bisection); False = FP64 every step
+    bisection_fp32_bracket: bool = True
     export: bool = False
 
     @classmethod

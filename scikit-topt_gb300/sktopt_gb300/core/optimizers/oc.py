@@ -56,7 +56,8 @@ class OC_Optimizer(DensityMethod):
                          beta_eta=cfg.beta_eta, scaling_min=cfg.scaling_rate_min,
                          scaling_max=cfg.scaling_rate_max, vol_tol=1e-4,
                          l1=cfg.lambda_lower, l2=cfg.lambda_upper, tolerance=1e-5,
-                         max_iter=1000)
+                         max_iter=1000,
+                         flags=0 if cfg.bisection_fp32_bracket else N.TOPT_OC_EXACT)
         lmid, verr, steps = flt.oc_bisect(st.dC_drho_full, self.running_scale, st.rho,
                                           self._vol_design, self._vol_design_sum, prm,
                                           st.scaling_rate)

@@ -97,6 +97,32 @@ def test_oc_loop_matches_oracle(native_lib):
         assert opt.kkt_residual == pytest.approx(ref.hist["kkt_residual"][-1], rel=1e-6)
 
 
+def test_oc_fp32_bracketed_bisection_equals_fp64(native_lib):
+    """FP32-bracketed bisection takes the FP64 bisection's path: identical
+    lmid, volume error, step count and density at every iteration."""
+    import dataclasses
+    from sktopt_gb300.core import OC_Optimizer
+    from sktopt_gb300.mesh import toy_problem
+    runs = []
+    for bracket in (True, False):
+        cfg = dataclasses.replace(_oc_cfg(6), bisection_fp32_bracket=bracket)
+        opt = OC_Optimizer(cfg, toy_problem.cantilever(24, 12, 12), device=_dev())
+        opt.parameterize()
+        steps, rhos = [], []
+        for _ in range(6):
+            opt.optimize_steps(1)
+            steps.append(opt.last_bisection_steps)
+            rhos.append(opt._state.rho.cpu().numpy().copy())
+        runs.append((opt.recorder.histories["lmid"], opt.recorder.histories["vol_error"],
+                     steps, rhos))
+    (l_a, v_a, s_a, r_a), (l_b, v_b, s_b, r_b) = runs
+    assert list(l_a) == list(l_b)
+    assert list(v_a) == list(v_b)
+    assert s_a == s_b
+    for a, b in zip(r_a, r_b):
+        assert np.array_equal(a, b)
+
+
 def test_oc_steps_equal_full_run_bitwise(native_lib):
     """The reference's determinism property (test_optimize_steps_equivalence.py:49)."""
     from sktopt_gb300.core import OC_Optimizer
