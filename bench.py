@@ -283,7 +283,9 @@ def run_gpu(args):
         "data": "synthetic (cantilever generated in-process)",
         "config": {"workload": f"OC loop, {size[0]}x{size[1]}x{size[2]} hex cantilever "
                                f"({size[0]*size[1]*size[2]} elements), Gaussian filter r=1.5, "
-                               "SIMP p=3, vf=0.3, move 0.2, MG-preconditioned mixed FCG to 1e-8",
+                               "SIMP p=3, vf=0.3, move 0.2, FP64 flexible CG with FP32 "
+                               "multigrid and FP32 operator, FP64 residual replacement, "
+                               "to 1e-8",
                    "parallelism": f"replicas x{world}",
                    "l2": "working set (>4 GB per step) exceeds the 129 MB L2"},
         "e2e": e2e, "gpu_launches": int(launches),

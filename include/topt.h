@@ -108,12 +108,16 @@ typedef struct topt_solve_opts {
                              inner work; FP64 residual, update and dots):
                              1: FP32 PCG with FP64 reliable updates;
                              2: FP32 PCG restarted inside FP64 refinement;
-                             3: FP64 flexible CG around an FP32 V-cycle   */
+                             3: FP64 flexible CG around an FP32 V-cycle;
+                             4: as 3 with the FP32 operator for the search
+                                products and FP64 residual replacement    */
   int32_t precond;        /* 0: block Jacobi; 1: multigrid V-cycle           */
   double rtol;            /* relative residual target (solver_elastic.py:37) */
   int32_t maxiter;        /* iteration cap (per inner solve for method 2)    */
-  double inner_rtol;      /* 1: residual drop between updates; 2: inner tol  */
-  int32_t max_outer;      /* 1, 2: cap on FP64 refinement steps              */
+  double inner_rtol;      /* 1, 4: residual drop between updates; 2: inner
+                             tolerance                                       */
+  int32_t max_outer;      /* 1, 2: cap on FP64 refinement steps; 4: most
+                             iterations between residual replacements       */
   int32_t cheb_degree;    /* Chebyshev smoother degree                       */
   int32_t check_every;    /* residual check period (iterations)              */
 } topt_solve_opts;

@@ -921,7 +921,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
   int slot_old = 3, slot_new = 4;
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, slot_new))) return rc;
   TOPT_L_DISPATCH(L, (k_pcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                         n, h->red.res(slot_new), h->red.res(slot_old), 1, z32, p32)));
+                         n, h->red.res(slot_new), h->red.res(slot_old), 1, z32, p32, nullptr)));
   std::swap(slot_old, slot_new);
   inf->status = TOPT_MAXITER;
   inf->iters = 0;
@@ -929,7 +929,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
   const float* A32 = H.lv[0].vals.as<float>();
   for (int it = 1; it <= maxiter; ++it) {
     if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_update<float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_pcg_update<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p32, q32,
                            x32, r32, h->red.partials.as<double>(), h->red.ctr(6),
                            h->red.res(6), nullptr)));
@@ -971,7 +971,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
     }
     if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, slot_new))) return rc;
     TOPT_L_DISPATCH(L, (k_pcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                           n, h->red.res(slot_new), h->red.res(slot_old), 0, z32, p32)));
+                           n, h->red.res(slot_new), h->red.res(slot_old), 0, z32, p32, nullptr)));
     std::swap(slot_old, slot_new);
   }
   TOPT_CUDA(cudaStreamSynchronize(h->stream));
@@ -1009,7 +1009,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   };
   if ((rc = apply_prec(slot_new))) return rc;
   TOPT_L_DISPATCH(L, (k_pcg_direction<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                         n, h->red.res(slot_new), h->red.res(slot_old), 1, z, p)));
+                         n, h->red.res(slot_new), h->red.res(slot_old), 1, z, p, nullptr)));
   std::swap(slot_old, slot_new);
   int it = 0;
   double rr[4] = {0, 0, 0, 0};
@@ -1018,7 +1018,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   for (it = 1; it <= maxiter; ++it) {
     // q = A p, pq = p.q
     if ((rc = spmv<T>(h, L0, bs, L, 0, true, vals, p, nullptr, q, 5))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_update<T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_pcg_update<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p, q, x, r,
                            h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), nullptr)));
     TOPT_CHECK_LAUNCH("k_pcg_update");
@@ -1038,7 +1038,7 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
     }
     if ((rc = apply_prec(slot_new))) return rc;
     TOPT_L_DISPATCH(L, (k_pcg_direction<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                           n, h->red.res(slot_new), h->red.res(slot_old), 0, z, p)));
+                           n, h->red.res(slot_new), h->red.res(slot_old), 0, z, p, nullptr)));
     std::swap(slot_old, slot_new);
   }
   *iters_out = std::min(it, maxiter);
@@ -1078,21 +1078,21 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   TOPT_CHECK_LAUNCH("k_convert");
   // z = M32(r); slot 3 <- r.z (FP64 r, FP32 z)
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
-  TOPT_L_DISPATCH(L, (k_dot2<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+  TOPT_L_DISPATCH(L, (k_dot2<double, double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                          n, r, r, z32, h->red.partials.as<double>(), h->red.ctr(8),
                          h->red.res(8))));
   TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
                             cudaMemcpyDeviceToDevice, h->stream));
   TOPT_L_DISPATCH(L, (k_pcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
                                                            h->stream>>>(
-                         n, h->red.res(3), h->red.res(3), 1, z32, p)));
+                         n, h->red.res(3), h->red.res(3), 1, z32, p, nullptr)));
   inf->status = TOPT_MAXITER;
   double rel = 1.0;
   int it;
   for (it = 1; it <= maxiter; ++it) {
     // q = A p, pq = p.q (slot 5); x += a p, r -= a q, r32 = float(r), rr (slot 6)
     if ((rc = spmv<double>(h, L0, bs, L, 0, true, A64, p, nullptr, q, 5))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_update<double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_pcg_update<double, double, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(3), h->red.res(5), active.as<int>(), p, q, U, r,
                            h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), r32)));
     TOPT_CHECK_LAUNCH("k_pcg_update");
@@ -1112,18 +1112,124 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
     }
     if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
     // slot 8 <- (r.z_new, q.z_new); slot 3 <- r.z_new
-    TOPT_L_DISPATCH(L, (k_dot2<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+    TOPT_L_DISPATCH(L, (k_dot2<double, double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, r, q, z32, h->red.partials.as<double>(), h->red.ctr(8),
                            h->red.res(8))));
     TOPT_L_DISPATCH(L, (k_fcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
                                                              h->stream>>>(
-                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p)));
+                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p, nullptr)));
     TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
                               cudaMemcpyDeviceToDevice, h->stream));
     TOPT_CHECK_LAUNCH("k_fcg_direction");
   }
   inf->iters = std::min(it, maxiter);
   inf->outer = inf->iters;
+  inf->relres = rel;
+  TOPT_CUDA(cudaStreamSynchronize(h->stream));
+  return TOPT_OK;
+}
+
+// Flexible CG in FP64 (solution, residual, directions, dots) with the FP32
+// level-0 operator for the search-direction products, preconditioned by the
+// FP32 V-cycle (or block Jacobi).  The recursive residual r -= alpha A32 p
+// drifts from Fe - A64 U by the FP32 operator error, so it is replaced by the
+// FP64 residual (one FP64 product) whenever it has dropped by `delta` since
+// the last replacement, after `max_between` iterations, and whenever it looks
+// converged: convergence is declared on the replaced FP64 residual only
+// (residual replacement, van der Vorst & Ye, SIAM J. Sci. Comput. 22, 2000).
+// Buffers: p, r FP64; q32, p32, r32, z32 FP32.
+static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* p, double* r, float* q32,
+                      float* p32, float* r32, float* z32, double rtol, int maxiter,
+                      int precond, int degree, double delta, int max_between,
+                      topt_solve_info* inf) {
+  Hier<float>& H = h->h32;
+  LevelStruct& L0 = h->ls[0];
+  const int bs = h->bs;
+  const int64_t n = h->n_dof, nl = n * L;
+  const double* fe = h->fe.as<double>();
+  const double* A64 = h->vals64_0.as<double>();
+  const float* A32 = H.lv[0].vals.as<float>();
+  int rc;
+  double bn2[4] = {0, 0, 0, 0}, rr[4], rlast2[4];
+  if ((rc = dot<double>(h, n, L, fe, fe, 2))) return rc;
+  if ((rc = read_slot(h, 2, L, bn2))) return rc;
+  int active_h[4] = {1, 1, 1, 1};
+  for (int j = 0; j < L; ++j) {
+    if (!(bn2[j] > 0.0)) active_h[j] = 0;
+    rlast2[j] = bn2[j];
+  }
+  DevBuf active;
+  if ((rc = upload(active, active_h, 4, h->stream))) return rc;
+  TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
+  TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice, h->stream));
+  k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
+  TOPT_CHECK_LAUNCH("k_convert");
+  if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
+  TOPT_L_DISPATCH(L, (k_dot2<double, double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                         n, r, r, z32, h->red.partials.as<double>(), h->red.ctr(8),
+                         h->red.res(8))));
+  TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
+                            cudaMemcpyDeviceToDevice, h->stream));
+  TOPT_L_DISPATCH(L, (k_pcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                           h->stream>>>(
+                         n, h->red.res(3), h->red.res(3), 1, z32, p, p32)));
+  inf->status = TOPT_MAXITER;
+  inf->outer = 0;
+  double rel = 1.0;
+  int it, since = 0;
+  for (it = 1; it <= maxiter; ++it) {
+    // q32 = A32 p32 and p.q (slot 5); U += a p, r -= a q32, r32, r.r (slot 6)
+    if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5))) return rc;
+    TOPT_L_DISPATCH(L, (k_pcg_update<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                           n, h->red.res(3), h->red.res(5), active.as<int>(), p, q32, U, r,
+                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), r32)));
+    TOPT_CHECK_LAUNCH("k_pcg_update");
+    ++since;
+    if ((rc = read_slot(h, 6, L, rr))) return rc;
+    bool small = true, dropped = false, bad = false;
+    for (int j = 0; j < L; ++j) {
+      if (!std::isfinite(rr[j])) bad = true;
+      if (!active_h[j]) continue;
+      if (rr[j] > rtol * rtol * bn2[j]) small = false;
+      if (rr[j] <= delta * delta * rlast2[j]) dropped = true;
+    }
+    if (bad) { inf->status = TOPT_NONFINITE; break; }
+    if (small || dropped || since >= max_between || it == maxiter) {
+      // residual replacement: r = Fe - A64 U in FP64
+      if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r))) return rc;
+      k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r, r32);
+      TOPT_CHECK_LAUNCH("k_convert");
+      if ((rc = dot<double>(h, n, L, r, r, 7))) return rc;
+      if ((rc = read_slot(h, 7, L, rr))) return rc;
+      inf->outer += 1;
+      since = 0;
+      bool done = true;
+      rel = 0.0;
+      for (int j = 0; j < L; ++j) {
+        if (!std::isfinite(rr[j])) bad = true;
+        rlast2[j] = rr[j];
+        if (!active_h[j]) continue;
+        const double rj = std::sqrt(rr[j] / bn2[j]);
+        rel = std::max(rel, rj);
+        if (rj > rtol) done = false;
+      }
+      if (bad) { inf->status = TOPT_NONFINITE; break; }
+      if (done) { inf->status = TOPT_OK; break; }
+    }
+    if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
+    // slot 8 <- (r.z_new, q.z_new); slot 3 <- r.z_new
+    TOPT_L_DISPATCH(L, (k_dot2<double, float, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                          h->stream>>>(
+                           n, r, q32, z32, h->red.partials.as<double>(), h->red.ctr(8),
+                           h->red.res(8))));
+    TOPT_L_DISPATCH(L, (k_fcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                             h->stream>>>(
+                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p, p32)));
+    TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
+                              cudaMemcpyDeviceToDevice, h->stream));
+    TOPT_CHECK_LAUNCH("k_fcg_direction");
+  }
+  inf->iters = std::min(it, maxiter);
   inf->relres = rel;
   TOPT_CUDA(cudaStreamSynchronize(h->stream));
   return TOPT_OK;
@@ -1344,8 +1450,8 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
   if (!h || !F || !U || !o) return fail(TOPT_BAD_INPUT, "fem_solve: null argument");
   if (!h->assembled) return fail(TOPT_BAD_INPUT, "fem_solve: call topt_fem_update first");
   if (nrhs < 1 || nrhs > 4) return fail(TOPT_BAD_INPUT, "fem_solve: nrhs must be 1..4");
-  if (o->method < 0 || o->method > 3)
-    return fail(TOPT_BAD_INPUT, "fem_solve: method must be 0..3");
+  if (o->method < 0 || o->method > 4)
+    return fail(TOPT_BAD_INPUT, "fem_solve: method must be 0..4");
   if (o->method >= 1 && !h->mixed)
     return fail(TOPT_BAD_INPUT, "fem_solve: mixed methods need a handle created with mixed=1");
   if (o->method == 0 && h->mixed)
@@ -1375,6 +1481,16 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
     float* r32 = (float*)h->R.p;
     if ((rc = pcg_fcg_mixed(h, L, U, p, q, r, r32, r32 + nl, o->rtol, o->maxiter, o->precond,
                             degree, check, &inf)))
+      return rc;
+  } else if (o->method == 4) {
+    // FP64 flexible CG with the FP32 operator and FP64 residual replacement;
+    // U0 holds p, r (FP64) and q32, p32 (FP32, in the q and z slots); R holds
+    // the FP32 r and z.
+    float* r32 = (float*)h->R.p;
+    const double delta = (o->inner_rtol > 0.0 && o->inner_rtol < 1.0) ? o->inner_rtol : 0.1;
+    const int max_between = o->max_outer > 0 ? o->max_outer : 50;
+    if ((rc = pcg_fcg_rr(h, L, U, p, r, (float*)q, (float*)z, r32, r32 + nl, o->rtol,
+                         o->maxiter, o->precond, degree, delta, max_between, &inf)))
       return rc;
   } else if (o->method == 1) {
     float* p32 = (float*)p;

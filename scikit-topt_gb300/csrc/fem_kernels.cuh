@@ -210,9 +210,9 @@ k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
             const T* __restrict__ b, T* __restrict__ y, double* partials, unsigned* counter,
             double* dot_out, ChebEp<T> ep) {
   TOPT_KERNEL_COUNT();
-  double dacc[L];
+  T tacc[L];
 #pragma unroll
-  for (int j = 0; j < L; ++j) dacc[j] = 0.0;
+  for (int j = 0; j < L; ++j) tacc[j] = T(0);
   const int64_t nthreads = (int64_t)gridDim.x * blockDim.x;
   for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
        row < ((sp.nrows + 31) & ~(int64_t)31); row += nthreads) {
@@ -248,12 +248,15 @@ k_sell_spmv(SellT sp, const T* __restrict__ vals, const T* __restrict__ x,
         else out = y[idx] - acc[i];
         y[idx] = out;
         acc[i] = out;
-        if (DOT) dacc[i % L] += (double)x[idx] * (double)out;
+        if (DOT) tacc[i % L] += x[idx] * out;
       }
       if (ep.kind) cheb_epilogue<T, BS, L>(ep, row, acc);
     }
   }
   if (DOT) {
+    double dacc[L];
+#pragma unroll
+    for (int j = 0; j < L; ++j) dacc[j] = (double)tacc[j];
     __shared__ double sh[32 * L];
     block_sum<double, L>(dacc, sh);
     grid_finish<double, L>(dacc, partials, counter, dot_out);
@@ -436,7 +439,7 @@ k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ 
     for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
   }
   const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
-  double dacc[1] = {0.0};
+  float tacc = 0.0f;
   if (iy < ny1 && ix < nx1 && iz < nz1) {
     const int a = iy + ny1 * (ix + nx1 * iz);
     const int ma = nmask ? nmask[a] : 0;
@@ -451,11 +454,12 @@ k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ 
       else out = y[idx] - ax;
       y[idx] = out;
       acc[c] = out;
-      if (DOT) dacc[0] += (double)x[idx] * (double)out;
+      if (DOT) tacc += x[idx] * out;
     }
     if (ep.kind) cheb_epilogue<float, 3, 1>(ep, a, acc);
   }
   if (DOT) {
+    double dacc[1] = {(double)tacc};
     __shared__ double sh[32];
     block_sum<double, 1>(dacc, sh);
     grid_finish<double, 1>(dacc, partials, counter, dot_out);
@@ -732,10 +736,10 @@ __global__ void k_dot(int64_t n, const T* __restrict__ x, const T* __restrict__ 
 
 // PCG update: alpha_j = rz_j / pq_j (0 when frozen or pq <= 0);
 // x += alpha p; r -= alpha q; partial sums of r.r; r32 (optional) = float(r).
-template <typename T, int L>
+template <typename T, typename TQ, int L>
 __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
                              const double* __restrict__ pq, const int* __restrict__ active,
-                             const T* __restrict__ p, const T* __restrict__ q,
+                             const T* __restrict__ p, const TQ* __restrict__ q,
                              T* __restrict__ x, T* __restrict__ r, double* partials,
                              unsigned* counter, double* rr_out, float* __restrict__ r32) {
   TOPT_KERNEL_COUNT();
@@ -754,7 +758,7 @@ __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
     for (int j = 0; j < L; ++j) {
       const int64_t q_ = i * L + j;
       x[q_] += alpha[j] * p[q_];
-      const T rv = r[q_] - alpha[j] * q[q_];
+      const T rv = r[q_] - alpha[j] * (T)q[q_];
       r[q_] = rv;
       if (r32) r32[q_] = (float)rv;
       acc[j] += (double)rv * (double)rv;
@@ -766,8 +770,8 @@ __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
 }
 
 // Two dots sharing z: out[0..L) = r.z, out[L..2L) = q.z (flexible CG).
-template <typename T, typename TZ, int L>
-__global__ void k_dot2(int64_t n, const T* __restrict__ r, const T* __restrict__ q,
+template <typename T, typename TQ, typename TZ, int L>
+__global__ void k_dot2(int64_t n, const T* __restrict__ r, const TQ* __restrict__ q,
                        const TZ* __restrict__ z, double* partials, unsigned* counter,
                        double* out) {
   TOPT_KERNEL_COUNT();
@@ -793,7 +797,8 @@ __global__ void k_dot2(int64_t n, const T* __restrict__ r, const T* __restrict__
 template <typename T, typename TZ, int L>
 __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
                                 const double* __restrict__ pq, const int* __restrict__ active,
-                                const TZ* __restrict__ z, T* __restrict__ p) {
+                                const TZ* __restrict__ z, T* __restrict__ p,
+                                float* __restrict__ p32) {
   TOPT_KERNEL_COUNT();
   T beta[L];
 #pragma unroll
@@ -802,7 +807,11 @@ __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int j = 0; j < L; ++j) p[i * L + j] = (T)z[i * L + j] + beta[j] * p[i * L + j];
+    for (int j = 0; j < L; ++j) {
+      const T v = (T)z[i * L + j] + beta[j] * p[i * L + j];
+      p[i * L + j] = v;
+      if (p32) p32[i * L + j] = (float)v;
+    }
   }
 }
 
@@ -810,7 +819,8 @@ __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
 template <typename T, typename TZ, int L>
 __global__ void k_pcg_direction(int64_t n, const double* __restrict__ rz_new,
                                 const double* __restrict__ rz_old, int first,
-                                const TZ* __restrict__ z, T* __restrict__ p) {
+                                const TZ* __restrict__ z, T* __restrict__ p,
+                                float* __restrict__ p32) {
   TOPT_KERNEL_COUNT();
   T beta[L];
 #pragma unroll
@@ -819,8 +829,11 @@ __global__ void k_pcg_direction(int64_t n, const double* __restrict__ rz_new,
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
-    for (int j = 0; j < L; ++j)   // p = z exactly on the first step (p may hold garbage)
-      p[i * L + j] = first ? (T)z[i * L + j] : (T)z[i * L + j] + beta[j] * p[i * L + j];
+    for (int j = 0; j < L; ++j) {   // p = z exactly on the first step (p may hold garbage)
+      const T v = first ? (T)z[i * L + j] : (T)z[i * L + j] + beta[j] * p[i * L + j];
+      p[i * L + j] = v;
+      if (p32) p32[i * L + j] = (float)v;
+    }
   }
 }
 

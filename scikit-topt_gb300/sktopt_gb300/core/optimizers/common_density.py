@@ -95,7 +95,7 @@ class DensityMethodConfig:
     precision: Literal["fp64", "mixed"] = "fp64"
     precond: Literal["mg", "jacobi", "auto"] = "auto"
     solver_rtol: float = 1e-8
-    inner_rtol: float = 1e-4
+    inner_rtol: float = 1e-1
     # OC bisection: FP32 evaluation of each step, FP64 only near a decision
     # edge (same result as the all-FP64 bisection); False = FP64 every step
     bisection_fp32_bracket: bool = True

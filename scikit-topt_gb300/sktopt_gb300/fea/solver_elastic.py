@@ -7,9 +7,13 @@ fields (solver_elastic.py:34-40) and adds the GPU choices:
 
 * ``precision``: "fp64" (plain FP64 PCG) or "mixed" (FP32 operator, FP32
   multigrid and FP32 inner work; FP64 residual, solution update and dots).
-  ``refine`` picks the refinement scheme: "fcg" (default) is Krylov-
-  accelerated refinement -- an FP64 flexible CG whose inner solve is one FP32
-  V-cycle on the rounded residual; "reliable" runs the CG recurrences in FP32
+  ``refine`` picks the refinement scheme: "replace" (default) is an FP64
+  flexible CG whose preconditioner is one FP32 V-cycle on the rounded
+  residual and whose search-direction products use the FP32 operator; the
+  FP64 residual Fe - K U is recomputed whenever the recursive one has dropped
+  by ``inner_rtol`` and before convergence is declared.  "fcg" is the same
+  flexible CG with the FP64 operator in every iteration; "reliable" runs the
+  CG recurrences in FP32
   and replaces the FP32 residual by the FP64 one whenever it has dropped by
   ``inner_rtol``; "restart" restarts an FP32 PCG to ``inner_rtol`` for every
   FP64 refinement step.
@@ -46,7 +50,7 @@ class LinearSolverConfig:
     allow_fallback_to_spsolve: bool = False
     precision: Literal["fp64", "mixed"] = "fp64"
     precond: Literal["mg", "jacobi", "auto"] = "auto"
-    refine: Literal["fcg", "reliable", "restart"] = "fcg"
+    refine: Literal["fcg", "replace", "reliable", "restart"] = "replace"
     inner_rtol: float = 1e-1
     max_outer: int = 30
     cheb_degree: int = 2
@@ -151,7 +155,7 @@ class FEM_SimpLinearElasticity:
         eng = self.engine
         F = self.forces(force_scale)
         method = 0 if cfg.precision != "mixed" else \
-            {"fcg": 3, "reliable": 1, "restart": 2}[cfg.refine]
+            {"fcg": 3, "replace": 4, "reliable": 1, "restart": 2}[cfg.refine]
         precond = 1 if eng.multigrid else 0
         comp, st = eng.solve(F, U, method, precond, cfg.resolved_rtol(),
                              cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,

@@ -79,7 +79,7 @@ class FEM_SimpLinearHeatConduction:
         cfg = self.solver_config
         eng = self.engine
         method = 0 if cfg.precision != "mixed" else \
-            {"fcg": 3, "reliable": 1, "restart": 2}[cfg.refine]
+            {"fcg": 3, "replace": 4, "reliable": 1, "restart": 2}[cfg.refine]
         _, st = eng.solve(self._F, U, method, 1 if eng.multigrid else 0, cfg.resolved_rtol(),
                           cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
                           cfg.cheb_degree, cfg.check_every)
