@@ -101,6 +101,7 @@ struct topt_fem {
   // matrix-free FP32 level-0 operator (uniform hex grid, shared unit matrix)
   bool mf = false;
   topt::MfGrid mfg{};
+  int mf_ty = 32;                      // y extent of the operator's node tiles
   topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
 };
 
@@ -340,6 +341,13 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 // whenever another handle's K0 was loaded last.
 static const void* g_k0_owner = nullptr;
 
+template <int TY, int MODE, bool DOT>
+static void launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  k_mf_tile<TY, MODE, DOT><<<(int)mf_tiles(h->mfg, TY), kMfThreads, 0, h->stream>>>(
+      h->mfg, h->coef32.as<float>(), h->nmask.as<uint8_t>(), x, b, y,
+      h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
+}
+
 template <int L, int MODE, bool DOT>
 static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot,
                      const ChebEp<float>& ep) {
@@ -349,10 +357,15 @@ static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int 
                                         cudaMemcpyDeviceToDevice, h->stream));
       g_k0_owner = h->ke32.p;
     }
-    k_mf_tile<MODE, DOT><<<(int)mf_tiles(h->mfg), kMfThreads, 0, h->stream>>>(
-        h->mfg, h->coef32.as<float>(), h->nmask.as<uint8_t>(), x, b, y,
-        h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot), ep);
+    if (h->mf_ty == 27) launch_mf_tile<27, MODE, DOT>(h, x, b, y, slot);
+    else if (h->mf_ty == 16) launch_mf_tile<16, MODE, DOT>(h, x, b, y, slot);
+    else launch_mf_tile<32, MODE, DOT>(h, x, b, y, slot);
     TOPT_CHECK_LAUNCH("k_mf_tile");
+    if (ep.kind) {
+      k_cheb_step<float, 3, 1><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(h->n_nodes,
+                                                                                 ep, y);
+      TOPT_CHECK_LAUNCH("k_cheb_step");
+    }
     return TOPT_OK;
   }
   k_mf_apply<float, L, MODE, DOT><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
@@ -1343,8 +1356,10 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
       if ((rc = upload(h->nmask, nm.data(), nm.size(), s))) return rc;
       TOPT_CUDA(cudaStreamSynchronize(s));
       // one grid-reduction partial per tile of the fused p.Ap variant
-      if (mf_tiles(h->mfg) > h->red.max_blocks &&
-          (rc = h->red.init((int)std::min<int64_t>(mf_tiles(h->mfg), INT32_MAX / 8))))
+      h->mf_ty = mf_pick_ty(ny + 1);
+      const int64_t tiles = mf_tiles(h->mfg, h->mf_ty);
+      if (tiles > h->red.max_blocks &&
+          (rc = h->red.init((int)std::min<int64_t>(tiles, INT32_MAX / 8))))
         return rc;
     }
     if (h->ls.size() > 1) {

@@ -365,104 +365,152 @@ __host__ __device__ constexpr int hoff(int a, int d) {
   return d == 0 ? (0xD4 >> a) & 1 : (d == 1 ? (0xB2 >> a) & 1 : (0xE8 >> a) & 1);
 }
 
-// Tiled variant: a CTA owns a kMfTY x kMfTX x kMfTZ block of nodes (y
-// fastest, one node per thread).  It stages the node halo (x as float4 per
-// node, fixed DOFs and nodes outside the grid zeroed) and the coefficients of
-// every cell touching the tile (0 outside the grid) in shared memory with
-// coalesced loads, so the per-node work is branch-free: per cell, 8 LDS.128
-// of its nodes and 72 FFMA with constant-bank K0 operands.  Two CTAs per SM
-// overlap one tile's staging with the other's arithmetic.
-constexpr int kMfTY = 32, kMfTX = 4, kMfTZ = 2;
-constexpr int kMfThreads = kMfTY * kMfTX * kMfTZ;
-constexpr int kMfHY = kMfTY + 2, kMfHX = kMfTX + 2, kMfHZ = kMfTZ + 2;
-constexpr int kMfCY = kMfTY + 1, kMfCX = kMfTX + 1, kMfCZ = kMfTZ + 1;
+// Tiled variant: a CTA of 256 threads owns a TY x 8 x 4 block of nodes (y
+// fastest; TY picked per grid to waste the fewest threads) and each thread
+// computes TY/8 of its nodes.  The CTA stages the node halo -- x as float4
+// per node, fixed DOFs and nodes outside the grid zeroed, the node's fixed
+// flags in .w -- and the coefficients of every cell touching the tile (0
+// outside the grid) in shared memory with row-wise coalesced loads, so the
+// per-node work is branch-free: per cell, 8 LDS.128 of its nodes and 72 FFMA
+// with constant-bank K0 operands.  The MODE 1/2 operand of a node is loaded
+// before its arithmetic.  Two CTAs per SM overlap one tile's staging with the
+// other's arithmetic.  (A Chebyshev step fused here measured slower than a
+// separate pass: its loads stall this compute-bound kernel.)
+constexpr int kMfTX = 8, kMfTZ = 4, kMfThreads = 256;
 
-inline int64_t mf_tiles(const MfGrid& g) {
-  return (int64_t)((g.ny + kMfTY) / kMfTY) * ((g.nx + kMfTX) / kMfTX) *
-         ((g.nz + kMfTZ) / kMfTZ);
+template <int TY>
+struct MfTile {
+  static constexpr int HY = TY + 2, HX = kMfTX + 2, HZ = kMfTZ + 2;
+  static constexpr int CY = TY + 1, CX = kMfTX + 1, CZ = kMfTZ + 1;
+  static constexpr int NN = TY * kMfTX * kMfTZ;
+  static constexpr int NPT = (NN + kMfThreads - 1) / kMfThreads;
+};
+
+inline int mf_pick_ty(int ny1) {
+  int best = 32;
+  int64_t waste = -1;
+  for (int ty : {32, 27, 16}) {
+    const int64_t w = (int64_t)((ny1 + ty - 1) / ty) * ty - ny1;
+    if (waste < 0 || w < waste) { waste = w; best = ty; }
+  }
+  return best;
 }
 
-template <int MODE, bool DOT>
+inline int64_t mf_tiles(const MfGrid& g, int ty) {
+  return (int64_t)((g.ny + ty) / ty) * ((g.nx + kMfTX) / kMfTX) * ((g.nz + kMfTZ) / kMfTZ);
+}
+
+template <int TY, int MODE, bool DOT>
 __global__ void __launch_bounds__(kMfThreads, 2)
 k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ nmask,
           const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
-          double* partials, unsigned* counter, double* dot_out, ChebEp<float> ep) {
+          double* partials, unsigned* counter, double* dot_out) {
   TOPT_KERNEL_COUNT();
-  __shared__ float4 xs[kMfHZ][kMfHX][kMfHY];
-  __shared__ float cs[kMfCZ][kMfCX][kMfCY];
+  using G = MfTile<TY>;
+  constexpr int TX = kMfTX, TZ = kMfTZ, NT = kMfThreads;
+  constexpr int HY = G::HY, HX = G::HX, HZ = G::HZ, CY = G::CY, CX = G::CX, CZ = G::CZ;
+  __shared__ float4 xs[HZ][HX][HY];
+  __shared__ float cs[CZ][CX][CY];
   const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
-  // 1-D grid of tiles, y tiles fastest (the block index is linear for the
-  // deterministic grid reduction)
-  const int nty = (ny1 + kMfTY - 1) / kMfTY, ntx = (nx1 + kMfTX - 1) / kMfTX;
+  // 1-D grid of tiles, y tiles fastest (linear block index for the grid reduction)
+  const int nty = (ny1 + TY - 1) / TY, ntx = (nx1 + TX - 1) / TX;
   const int bt = blockIdx.x;
-  const int ty = (bt % nty) * kMfTY, tx = ((bt / nty) % ntx) * kMfTX,
-            tz = (bt / (nty * ntx)) * kMfTZ;
-  for (int i = threadIdx.x; i < kMfHZ * kMfHX * kMfHY; i += kMfThreads) {
-    const int hy = i % kMfHY, hx = (i / kMfHY) % kMfHX, hz = i / (kMfHY * kMfHX);
-    const int jy = ty - 1 + hy, jx = tx - 1 + hx, jz = tz - 1 + hz;
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (jy >= 0 && jx >= 0 && jz >= 0 && jy < ny1 && jx < nx1 && jz < nz1) {
-      const int nb = jy + ny1 * (jx + nx1 * jz);
-      const int m = nmask ? nmask[nb] : 0;
-      v.x = (m & 1) ? 0.f : x[nb * 3 + 0];
-      v.y = (m & 2) ? 0.f : x[nb * 3 + 1];
-      v.z = (m & 4) ? 0.f : x[nb * 3 + 2];
+  const int ty = (bt % nty) * TY, tx = ((bt / nty) % ntx) * TX, tz = (bt / (nty * ntx)) * TZ;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int row = warp; row < HZ * HX; row += NT / 32) {
+    const int hz = row / HX, hx = row % HX;
+    const int jz = tz - 1 + hz, jx = tx - 1 + hx;
+    const bool rin = jz >= 0 && jz < nz1 && jx >= 0 && jx < nx1;
+    const int base = ny1 * (jx + nx1 * jz);
+    for (int hy = lane; hy < HY; hy += 32) {
+      const int jy = ty - 1 + hy;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (rin && jy >= 0 && jy < ny1) {
+        const int nb = base + jy;
+        const int m = nmask ? nmask[nb] : 0;
+        v.x = (m & 1) ? 0.f : x[nb * 3 + 0];
+        v.y = (m & 2) ? 0.f : x[nb * 3 + 1];
+        v.z = (m & 4) ? 0.f : x[nb * 3 + 2];
+        v.w = __int_as_float(m);
+      }
+      xs[hz][hx][hy] = v;
     }
-    xs[hz][hx][hy] = v;
   }
-  for (int i = threadIdx.x; i < kMfCZ * kMfCX * kMfCY; i += kMfThreads) {
-    const int cy = i % kMfCY, cx = (i / kMfCY) % kMfCX, cz = i / (kMfCY * kMfCX);
-    const int ey = ty - 1 + cy, ex = tx - 1 + cx, ez = tz - 1 + cz;
-    const bool in = ey >= 0 && ex >= 0 && ez >= 0 && ey < g.ny && ex < g.nx && ez < g.nz;
-    cs[cz][cx][cy] = in ? coef[ey + g.ny * (ex + g.nx * ez)] : 0.f;
+  for (int row = warp; row < CZ * CX; row += NT / 32) {
+    const int cz = row / CX, cx = row % CX;
+    const int ez = tz - 1 + cz, ex = tx - 1 + cx;
+    const bool rin = ez >= 0 && ez < g.nz && ex >= 0 && ex < g.nx;
+    const int base = g.ny * (ex + g.nx * ez);
+    for (int cy = lane; cy < CY; cy += 32) {
+      const int ey = ty - 1 + cy;
+      cs[cz][cx][cy] = (rin && ey >= 0 && ey < g.ny) ? coef[base + ey] : 0.f;
+    }
   }
   __syncthreads();
-  const int ly = threadIdx.x % kMfTY, lx = (threadIdx.x / kMfTY) % kMfTX,
-            lz = threadIdx.x / (kMfTY * kMfTX);
-  float acc[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-  for (int la = 0; la < 8; ++la) {
-    float part[3] = {0.0f, 0.0f, 0.0f};
-#pragma unroll
-    for (int lb = 0; lb < 8; ++lb) {
-      const float4 v = xs[lz + 1 - hoff(la, 2) + hoff(lb, 2)][lx + 1 - hoff(la, 0) + hoff(lb, 0)]
-                         [ly + 1 - hoff(la, 1) + hoff(lb, 1)];
-      const float xv[3] = {v.x, v.y, v.z};
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-          part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
-    }
-    const float s = cs[lz + 1 - hoff(la, 2)][lx + 1 - hoff(la, 0)][ly + 1 - hoff(la, 1)];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
-  }
-  const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
   float tacc = 0.0f;
-  if (iy < ny1 && ix < nx1 && iz < nz1) {
+#pragma unroll 1
+  for (int k = 0; k < G::NPT; ++k) {
+    const int li = threadIdx.x + k * NT;
+    if (li >= G::NN) break;
+    const int ly = li % TY, lx = (li / TY) % TX, lz = li / (TY * TX);
+    const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
+    if (iy >= ny1 || ix >= nx1 || iz >= nz1) continue;
     const int a = iy + ny1 * (ix + nx1 * iz);
-    const int ma = nmask ? nmask[a] : 0;
+    float bv[3] = {0.f, 0.f, 0.f};
+    if (MODE != 0) {
+      const float* src = MODE == 1 ? b : y;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) bv[c] = src[(int64_t)a * 3 + c];
+    }
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int la = 0; la < 8; ++la) {
+      float part[3] = {0.0f, 0.0f, 0.0f};
+#pragma unroll
+      for (int lb = 0; lb < 8; ++lb) {
+        const float4 v = xs[lz + 1 - hoff(la, 2) + hoff(lb, 2)][lx + 1 - hoff(la, 0) + hoff(lb, 0)]
+                           [ly + 1 - hoff(la, 1) + hoff(lb, 1)];
+        const float xv[3] = {v.x, v.y, v.z};
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+#pragma unroll
+          for (int d = 0; d < 3; ++d)
+            part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
+      }
+      const float s = cs[lz + 1 - hoff(la, 2)][lx + 1 - hoff(la, 0)][ly + 1 - hoff(la, 1)];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
+    }
     // fixed rows act as identity rows (the staged x of a fixed DOF is 0)
+    const int ma = __float_as_int(xs[lz + 1][lx + 1][ly + 1].w);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const int64_t idx = (int64_t)a * 3 + c;
       const float ax = ((ma >> c) & 1) ? x[idx] : acc[c];
-      float out;
-      if (MODE == 0) out = ax;
-      else if (MODE == 1) out = b[idx] - ax;
-      else out = y[idx] - ax;
+      const float out = MODE == 0 ? ax : bv[c] - ax;
       y[idx] = out;
-      acc[c] = out;
       if (DOT) tacc += x[idx] * out;
     }
-    if (ep.kind) cheb_epilogue<float, 3, 1>(ep, a, acc);
   }
   if (DOT) {
     double dacc[1] = {(double)tacc};
     __shared__ double sh[32];
     block_sum<double, 1>(dacc, sh);
     grid_finish<double, 1>(dacc, partials, counter, dot_out);
+  }
+}
+
+// Chebyshev step as a separate pass (after an operator kernel that wrote r),
+// per node: the ChebEp update with dold and dnew allowed to coincide.
+template <typename T, int BS, int L>
+__global__ void k_cheb_step(int64_t n_nodes, ChebEp<T> ep, const T* __restrict__ r) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    T rv[BS * L];
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) rv[q] = r[i * BS * L + q];
+    cheb_epilogue<T, BS, L>(ep, i, rv);
   }
 }
 

@@ -2,7 +2,8 @@
 the CPU oracle (SciPy CSR + spsolve).
 
 Tolerances: assembled values 1e-13 relative to max |K|; FP64 PCG compliance
-1e-10 relative (solver rtol 1e-12); mixed refined compliance 1e-6 relative;
+1e-10 relative (solver rtol 1e-12); mixed refined compliance 1e-6 relative
+(displacements 1e-6 of max |U|); matrix-free FP32 operator 2e-6 of max |y|;
 energies and sensitivities 1e-9 relative L2 (they inherit the solve error).
 """
 import numpy as np
@@ -115,11 +116,40 @@ def test_mixed_refined_compliance(native_lib):
     eng.update(torch.from_numpy(rho).to(dev), 1.0, 1e-9, 3.0)
     F = torch.from_numpy(np.column_stack(tsk.neumann_linear)).to(dev)
     U = torch.zeros_like(F)
-    for method in (1, 2):   # reliable updates, restarted refinement
-        comp, st = eng.solve(F, U, method, 1, 1e-8, 500, inner_rtol=1e-1 if method == 1 else 1e-4)
-        assert st.status == 0, st
+    # 1 reliable updates, 2 restarted refinement, 3 flexible CG with the FP64
+    # operator, 4 flexible CG with the FP32 operator and residual replacement
+    for method in (1, 2, 3, 4):
+        comp, st = eng.solve(F, U, method, 1, 1e-8, 500,
+                             inner_rtol=1e-4 if method == 2 else 1e-1)
+        assert st.status == 0, (method, st)
         assert st.outer >= 1
-        assert abs(comp[0] - comp_ref[0]) <= 1e-6 * abs(comp_ref[0])
+        assert st.relres <= 1e-8
+        assert abs(comp[0] - comp_ref[0]) <= 1e-6 * abs(comp_ref[0]), method
+        np.testing.assert_allclose(U.cpu().numpy(), U_ref, rtol=0,
+                                   atol=1e-6 * np.abs(U_ref).max())
+
+
+@pytest.mark.parametrize("ny", [10, 26, 31])   # node tiles 16, 27 and 32 nodes high
+def test_matrix_free_operator_matches_assembled(native_lib, ny):
+    """FP32 matrix-free operator of a uniform hex grid vs the assembled FP32
+    matrix (same enforced operator, FP32 rounding apart)."""
+    import torch
+    from sktopt_gb300.fea import composer
+    from sktopt_gb300.fea.engine import FemEngine
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(9, ny, 5)
+    Ke, _, _ = composer.element_matrices(tsk.mesh, 0.3)
+    rho = torch.from_numpy(_rho(tsk.mesh.nelements, 11, lo=1e-3)).to(_dev())
+    x = torch.from_numpy(np.random.default_rng(12).standard_normal((3 * tsk.mesh.nnodes, 1)))
+    x32 = x.float().to(_dev())
+    out = []
+    for mf in (True, False):
+        eng = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True,
+                        matrix_free=mf)
+        eng.update(rho, 1.0, 1e-9, 3.0)
+        out.append(eng.spmv(x32, torch.float32).double().cpu().numpy())
+    ref = out[1]
+    np.testing.assert_allclose(out[0], ref, rtol=0, atol=2e-6 * np.abs(ref).max())
 
 
 def test_energy_and_sensitivity(native_lib):
@@ -158,7 +188,8 @@ def test_multi_load_block_rhs(native_lib):
     U_ref = ofem.solve(Ke_, Fe, "spsolve")
     comp_ref = np.einsum("ij,ij->j", Fe, U_ref)
     dev = _dev()
-    for mixed, method, tol in ((False, 0, 1e-10), (True, 1, 1e-6)):
+    for mixed, method, tol in ((False, 0, 1e-10), (True, 1, 1e-6), (True, 3, 1e-6),
+                               (True, 4, 1e-6)):
         eng = _engine_for(tsk, mixed=mixed)
         eng.update(torch.from_numpy(rho).to(dev), 1.0, 1e-9, 3.0)
         Ft = torch.from_numpy(np.ascontiguousarray(F)).to(dev)
