@@ -109,8 +109,9 @@ typedef struct topt_solve_opts {
                              1: FP32 PCG with FP64 reliable updates;
                              2: FP32 PCG restarted inside FP64 refinement;
                              3: FP64 flexible CG around an FP32 V-cycle;
-                             4: as 3 with the FP32 operator for the search
-                                products and FP64 residual replacement    */
+                             4: flexible CG with FP32 recurrences and
+                                operator, FP64 solution and FP64 residual
+                                replacement, around the FP32 V-cycle      */
   int32_t precond;        /* 0: block Jacobi; 1: multigrid V-cycle           */
   double rtol;            /* relative residual target (solver_elastic.py:37) */
   int32_t maxiter;        /* iteration cap (per inner solve for method 2)    */

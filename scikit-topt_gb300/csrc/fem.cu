@@ -1142,19 +1142,21 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   return TOPT_OK;
 }
 
-// Flexible CG in FP64 (solution, residual, directions, dots) with the FP32
-// level-0 operator for the search-direction products, preconditioned by the
-// FP32 V-cycle (or block Jacobi).  The recursive residual r -= alpha A32 p
-// drifts from Fe - A64 U by the FP32 operator error, so it is replaced by the
-// FP64 residual (one FP64 product) whenever it has dropped by `delta` since
-// the last replacement, after `max_between` iterations, and whenever it looks
-// converged: convergence is declared on the replaced FP64 residual only
-// (residual replacement, van der Vorst & Ye, SIAM J. Sci. Comput. 22, 2000).
-// Buffers: p, r FP64; q32, p32, r32, z32 FP32.
-static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* p, double* r, float* q32,
-                      float* p32, float* r32, float* z32, double rtol, int maxiter,
-                      int precond, int degree, double delta, int max_between,
-                      topt_solve_info* inf) {
+// Flexible CG with FP32 recurrences (residual, directions, products with the
+// FP32 level-0 operator, dots accumulated in FP64 across threads) and the
+// solution accumulated in FP64, preconditioned by the FP32 V-cycle (or block
+// Jacobi).  The recursive FP32 residual drifts from Fe - A64 U by the FP32
+// operator and rounding errors, so it is replaced by the FP64 residual (one
+// FP64 product, rounded to FP32) whenever it has dropped by `delta` since the
+// last replacement, after `max_between` iterations, and whenever it looks
+// converged; convergence is declared on the FP64 residual only (residual
+// replacement, van der Vorst & Ye, SIAM J. Sci. Comput. 22, 2000).  The
+// Polak-Ribiere direction update beta = -(q.z_new)/(p.q) tolerates both the
+// replacements and the FP32 inner solve.  Buffers: r64 FP64 (replacement
+// only); p32, q32, r32, z32 FP32.
+static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* r64, float* p32, float* q32,
+                      float* r32, float* z32, double rtol, int maxiter, int precond,
+                      int degree, double delta, int max_between, topt_solve_info* inf) {
   Hier<float>& H = h->h32;
   LevelStruct& L0 = h->ls[0];
   const int bs = h->bs;
@@ -1174,29 +1176,28 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* p, double* r, float
   DevBuf active;
   if ((rc = upload(active, active_h, 4, h->stream))) return rc;
   TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
-  TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice, h->stream));
   k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
   TOPT_CHECK_LAUNCH("k_convert");
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
-  TOPT_L_DISPATCH(L, (k_dot2<double, double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                         n, r, r, z32, h->red.partials.as<double>(), h->red.ctr(8),
+  TOPT_L_DISPATCH(L, (k_dot2<float, float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                         n, r32, r32, z32, h->red.partials.as<double>(), h->red.ctr(8),
                          h->red.res(8))));
   TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
                             cudaMemcpyDeviceToDevice, h->stream));
-  TOPT_L_DISPATCH(L, (k_pcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
-                                                           h->stream>>>(
-                         n, h->red.res(3), h->red.res(3), 1, z32, p, p32)));
+  TOPT_L_DISPATCH(L, (k_pcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                          h->stream>>>(
+                         n, h->red.res(3), h->red.res(3), 1, z32, p32, nullptr)));
   inf->status = TOPT_MAXITER;
   inf->outer = 0;
   double rel = 1.0;
   int it, since = 0;
   for (it = 1; it <= maxiter; ++it) {
-    // q32 = A32 p32 and p.q (slot 5); U += a p, r -= a q32, r32, r.r (slot 6)
+    // q32 = A32 p32 and p.q (slot 5); U += a p (FP64), r32 -= a q32, r.r (slot 6)
     if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5))) return rc;
-    TOPT_L_DISPATCH(L, (k_pcg_update<double, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
-                           n, h->red.res(3), h->red.res(5), active.as<int>(), p, q32, U, r,
-                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), r32)));
-    TOPT_CHECK_LAUNCH("k_pcg_update");
+    TOPT_L_DISPATCH(L, (k_fcg_update32<L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
+                           n, h->red.res(3), h->red.res(5), active.as<int>(), p32, q32, U, r32,
+                           h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6))));
+    TOPT_CHECK_LAUNCH("k_fcg_update32");
     ++since;
     if ((rc = read_slot(h, 6, L, rr))) return rc;
     bool small = true, dropped = false, bad = false;
@@ -1208,11 +1209,11 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* p, double* r, float
     }
     if (bad) { inf->status = TOPT_NONFINITE; break; }
     if (small || dropped || since >= max_between || it == maxiter) {
-      // residual replacement: r = Fe - A64 U in FP64
-      if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r))) return rc;
-      k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r, r32);
+      // residual replacement: r = Fe - A64 U in FP64, rounded to FP32
+      if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r64))) return rc;
+      k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r64, r32);
       TOPT_CHECK_LAUNCH("k_convert");
-      if ((rc = dot<double>(h, n, L, r, r, 7))) return rc;
+      if ((rc = dot<double>(h, n, L, r64, r64, 7))) return rc;
       if ((rc = read_slot(h, 7, L, rr))) return rc;
       inf->outer += 1;
       since = 0;
@@ -1231,13 +1232,14 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* p, double* r, float
     }
     if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
     // slot 8 <- (r.z_new, q.z_new); slot 3 <- r.z_new
-    TOPT_L_DISPATCH(L, (k_dot2<double, float, float, L_><<<gridsize(h, n), kBlock, 0,
-                                                          h->stream>>>(
-                           n, r, q32, z32, h->red.partials.as<double>(), h->red.ctr(8),
+    TOPT_L_DISPATCH(L, (k_dot2<float, float, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                         h->stream>>>(
+                           n, r32, q32, z32, h->red.partials.as<double>(), h->red.ctr(8),
                            h->red.res(8))));
-    TOPT_L_DISPATCH(L, (k_fcg_direction<double, float, L_><<<gridsize(h, n), kBlock, 0,
-                                                             h->stream>>>(
-                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p, p32)));
+    TOPT_L_DISPATCH(L, (k_fcg_direction<float, float, L_><<<gridsize(h, n), kBlock, 0,
+                                                            h->stream>>>(
+                           n, h->red.res(8) + L, h->red.res(5), active.as<int>(), z32, p32,
+                           nullptr)));
     TOPT_CUDA(cudaMemcpyAsync(h->red.res(3), h->red.res(8), sizeof(double) * L,
                               cudaMemcpyDeviceToDevice, h->stream));
     TOPT_CHECK_LAUNCH("k_fcg_direction");
@@ -1498,13 +1500,13 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
                             degree, check, &inf)))
       return rc;
   } else if (o->method == 4) {
-    // FP64 flexible CG with the FP32 operator and FP64 residual replacement;
-    // U0 holds p, r (FP64) and q32, p32 (FP32, in the q and z slots); R holds
-    // the FP32 r and z.
+    // flexible CG with FP32 recurrences, FP64 solution and FP64 residual
+    // replacement; U0 holds the FP64 replacement residual and p32, q32 (in
+    // the q slot); R holds the FP32 r and z.
     float* r32 = (float*)h->R.p;
     const double delta = (o->inner_rtol > 0.0 && o->inner_rtol < 1.0) ? o->inner_rtol : 0.1;
     const int max_between = o->max_outer > 0 ? o->max_outer : 50;
-    if ((rc = pcg_fcg_rr(h, L, U, p, r, (float*)q, (float*)z, r32, r32 + nl, o->rtol,
+    if ((rc = pcg_fcg_rr(h, L, U, r, (float*)q, (float*)q + nl, r32, r32 + nl, o->rtol,
                          o->maxiter, o->precond, degree, delta, max_between, &inf)))
       return rc;
   } else if (o->method == 1) {

@@ -817,24 +817,68 @@ __global__ void k_pcg_update(int64_t n, const double* __restrict__ rz,
   grid_finish<double, L>(acc, partials, counter, rr_out);
 }
 
+// Flexible CG update with FP32 recurrences and an FP64 solution:
+// alpha_j = rz_j / pq_j (0 when frozen or pq <= 0); U += alpha p (FP64);
+// r -= alpha q (FP32); partial sums of r.r.
+template <int L>
+__global__ void k_fcg_update32(int64_t n, const double* __restrict__ rz,
+                               const double* __restrict__ pq, const int* __restrict__ active,
+                               const float* __restrict__ p, const float* __restrict__ q,
+                               double* __restrict__ U, float* __restrict__ r, double* partials,
+                               unsigned* counter, double* rr_out) {
+  TOPT_KERNEL_COUNT();
+  double alpha[L];
+  float alpha32[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) {
+    const double d = pq[j];
+    alpha[j] = (active[j] && d > 0.0) ? rz[j] / d : 0.0;
+    alpha32[j] = (float)alpha[j];
+  }
+  float tacc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) tacc[j] = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      const int64_t q_ = i * L + j;
+      U[q_] += alpha[j] * (double)p[q_];
+      const float rv = r[q_] - alpha32[j] * q[q_];
+      r[q_] = rv;
+      tacc[j] += rv * rv;
+    }
+  }
+  double acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = (double)tacc[j];
+  __shared__ double sh[32 * L];
+  block_sum<double, L>(acc, sh);
+  grid_finish<double, L>(acc, partials, counter, rr_out);
+}
+
 // Two dots sharing z: out[0..L) = r.z, out[L..2L) = q.z (flexible CG).
 template <typename T, typename TQ, typename TZ, int L>
 __global__ void k_dot2(int64_t n, const T* __restrict__ r, const TQ* __restrict__ q,
                        const TZ* __restrict__ z, double* partials, unsigned* counter,
                        double* out) {
   TOPT_KERNEL_COUNT();
-  double acc[2 * L];
+  // per-thread sums in T (FP32 inputs need no FP64 arithmetic), then FP64
+  T tacc[2 * L];
 #pragma unroll
-  for (int j = 0; j < 2 * L; ++j) acc[j] = 0.0;
+  for (int j = 0; j < 2 * L; ++j) tacc[j] = T(0);
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
 #pragma unroll
     for (int j = 0; j < L; ++j) {
-      const double zv = (double)z[i * L + j];
-      acc[j] += (double)r[i * L + j] * zv;
-      acc[L + j] += (double)q[i * L + j] * zv;
+      const T zv = (T)z[i * L + j];
+      tacc[j] += (T)r[i * L + j] * zv;
+      tacc[L + j] += (T)q[i * L + j] * zv;
     }
   }
+  double acc[2 * L];
+#pragma unroll
+  for (int j = 0; j < 2 * L; ++j) acc[j] = (double)tacc[j];
   __shared__ double sh[32 * 2 * L];
   block_sum<double, 2 * L>(acc, sh);
   grid_finish<double, 2 * L>(acc, partials, counter, out);

@@ -7,13 +7,13 @@ fields (solver_elastic.py:34-40) and adds the GPU choices:
 
 * ``precision``: "fp64" (plain FP64 PCG) or "mixed" (FP32 operator, FP32
   multigrid and FP32 inner work; FP64 residual, solution update and dots).
-  ``refine`` picks the refinement scheme: "replace" (default) is an FP64
-  flexible CG whose preconditioner is one FP32 V-cycle on the rounded
-  residual and whose search-direction products use the FP32 operator; the
-  FP64 residual Fe - K U is recomputed whenever the recursive one has dropped
-  by ``inner_rtol`` and before convergence is declared.  "fcg" is the same
-  flexible CG with the FP64 operator in every iteration; "reliable" runs the
-  CG recurrences in FP32
+  ``refine`` picks the refinement scheme: "replace" (default) is a flexible
+  CG preconditioned by one FP32 V-cycle, with FP32 recurrences and operator
+  and the solution accumulated in FP64; the FP64 residual Fe - K U replaces
+  the recursive one whenever that has dropped by ``inner_rtol`` and before
+  convergence is declared.  "fcg" is an FP64 flexible CG (FP64 operator in
+  every iteration) around the same V-cycle; "reliable" runs the CG
+  recurrences in FP32
   and replaces the FP32 residual by the FP64 one whenever it has dropped by
   ``inner_rtol``; "restart" restarts an FP32 PCG to ``inner_rtol`` for every
   FP64 refinement step.
