@@ -102,6 +102,7 @@ struct topt_fem {
   bool mf = false;
   topt::MfGrid mfg{};
   int mf_ty = 32;                      // y extent of the operator's node tiles
+  topt::DevBuf nmask32;                // nmask widened to 32 bits (cp.async granule)
   topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
 };
 
@@ -341,26 +342,42 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 // whenever another handle's K0 was loaded last.
 static const void* g_k0_owner = nullptr;
 
-template <int TY, int MODE, bool DOT>
-static void launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y, int slot) {
-  k_mf_tile<TY, MODE, DOT><<<(int)mf_tiles(h->mfg, TY), kMfThreads, 0, h->stream>>>(
-      h->mfg, h->coef32.as<float>(), h->nmask.as<uint8_t>(), x, b, y,
+template <int TY, int MODE, bool DOT, bool COLMASK>
+static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  static bool attr_set = false;   // per instantiation, process-wide
+  if (!attr_set) {
+    TOPT_CUDA(cudaFuncSetAttribute(k_mf_tile<TY, MODE, DOT, COLMASK>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   MfTile<TY>::SMEM));
+    attr_set = true;
+  }
+  k_mf_tile<TY, MODE, DOT, COLMASK><<<h->sm * kMfCtasPerSm, kMfThreads, MfTile<TY>::SMEM,
+                                      h->stream>>>(
+      h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), x, b, y,
       h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
+  TOPT_CHECK_LAUNCH("k_mf_tile");
+  return TOPT_OK;
+}
+
+template <int MODE, bool DOT, bool COLMASK>
+static int launch_mf_ty(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  if (h->mf_ty == 27) return launch_mf_tile<27, MODE, DOT, COLMASK>(h, x, b, y, slot);
+  if (h->mf_ty == 16) return launch_mf_tile<16, MODE, DOT, COLMASK>(h, x, b, y, slot);
+  return launch_mf_tile<32, MODE, DOT, COLMASK>(h, x, b, y, slot);
 }
 
 template <int L, int MODE, bool DOT>
 static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot,
-                     const ChebEp<float>& ep) {
+                     const ChebEp<float>& ep, bool zero_fixed) {
   if (L == 1) {
     if (g_k0_owner != h->ke32.p) {
       TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->ke32.p, 576 * sizeof(float), 0,
                                         cudaMemcpyDeviceToDevice, h->stream));
       g_k0_owner = h->ke32.p;
     }
-    if (h->mf_ty == 27) launch_mf_tile<27, MODE, DOT>(h, x, b, y, slot);
-    else if (h->mf_ty == 16) launch_mf_tile<16, MODE, DOT>(h, x, b, y, slot);
-    else launch_mf_tile<32, MODE, DOT>(h, x, b, y, slot);
-    TOPT_CHECK_LAUNCH("k_mf_tile");
+    const int rc = zero_fixed ? launch_mf_ty<MODE, DOT, false>(h, x, b, y, slot)
+                              : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
+    if (rc) return rc;
     if (ep.kind) {
       k_cheb_step<float, 3, 1><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(h->n_nodes,
                                                                                  ep, y);
@@ -376,26 +393,28 @@ static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int 
 }
 
 static int mf_spmv(topt_fem* h, int L, int mode, bool dot, const float* x, const float* b,
-                   float* y, int slot, const ChebEp<float>& ep) {
+                   float* y, int slot, const ChebEp<float>& ep, bool zf) {
 #define TOPT_MF_CASE(L_)                                                            \
   if (L == L_) {                                                                    \
-    if (mode == 0 && !dot) return launch_mf<L_, 0, false>(h, x, b, y, slot, ep);    \
-    if (mode == 0 && dot) return launch_mf<L_, 0, true>(h, x, b, y, slot, ep);      \
-    if (mode == 1) return launch_mf<L_, 1, false>(h, x, b, y, slot, ep);            \
-    if (mode == 2) return launch_mf<L_, 2, false>(h, x, b, y, slot, ep);            \
+    if (mode == 0 && !dot) return launch_mf<L_, 0, false>(h, x, b, y, slot, ep, zf); \
+    if (mode == 0 && dot) return launch_mf<L_, 0, true>(h, x, b, y, slot, ep, zf);   \
+    if (mode == 1) return launch_mf<L_, 1, false>(h, x, b, y, slot, ep, zf);         \
+    if (mode == 2) return launch_mf<L_, 2, false>(h, x, b, y, slot, ep, zf);         \
   }
   TOPT_MF_CASE(1) TOPT_MF_CASE(2) TOPT_MF_CASE(3) TOPT_MF_CASE(4)
 #undef TOPT_MF_CASE
   return fail(TOPT_BAD_INPUT, "mf_spmv: unsupported nrhs");
 }
 
+// zero_fixed: x is known to vanish on the fixed DOFs (every operand inside the
+// solvers), so the matrix-free operator may skip zeroing them.
 template <typename T>
 static int spmv(topt_fem* h, const LevelStruct& Ls, int bs, int L, int mode, bool dot,
                 const T* vals, const T* x, const T* b, T* y, int slot = 0,
-                const ChebEp<T>& ep = ChebEp<T>()) {
+                const ChebEp<T>& ep = ChebEp<T>(), bool zero_fixed = false) {
   if (std::is_same<T, float>::value && h->mf && &Ls == &h->ls[0])
     return mf_spmv(h, L, mode, dot, (const float*)x, (const float*)b, (float*)y, slot,
-                   reinterpret_cast<const ChebEp<float>&>(ep));
+                   reinterpret_cast<const ChebEp<float>&>(ep), zero_fixed);
 #define TOPT_SPMV_CASE(BS_, L_)                                                        \
   if (bs == BS_ && L == L_) {                                                          \
     if (mode == 0 && !dot)                                                             \
@@ -778,11 +797,13 @@ static int smooth_pre(topt_fem* h, int li, Hier<T>& H, int L, int degree, const 
     ep.dold = dA;
     ep.dnew = dB;
     // step 1: r = b - A d (x == d); later steps: r -= A d
-    if ((rc = spmv<T>(h, Ls, h->bs, L, k == 1 ? 1 : 2, false, vals, dA, b, r, 0, ep))) return rc;
+    if ((rc = spmv<T>(h, Ls, h->bs, L, k == 1 ? 1 : 2, false, vals, dA, b, r, 0, ep, true)))
+      return rc;
     std::swap(dA, dB);
     rho0 = rho1;
   }
-  return spmv<T>(h, Ls, h->bs, L, degree == 1 ? 1 : 2, false, vals, dA, b, r);
+  return spmv<T>(h, Ls, h->bs, L, degree == 1 ? 1 : 2, false, vals, dA, b, r, 0, ChebEp<T>(),
+                 true);
 }
 
 // Post-smoothing of x (nonzero guess): r = b - A x fused with the first
@@ -804,7 +825,7 @@ static int smooth_post(topt_fem* h, int li, Hier<T>& H, int L, int degree, const
   ep.kind = 1;
   ep.c2 = (T)(1.0 / cp.theta);
   ep.dnew = dA;
-  if ((rc = spmv<T>(h, Ls, h->bs, L, 1, false, vals, x, b, r, 0, ep))) return rc;
+  if ((rc = spmv<T>(h, Ls, h->bs, L, 1, false, vals, x, b, r, 0, ep, true))) return rc;
   if (degree == 1) {
     k_axpy<T><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, T(1), dA, x);
     TOPT_CHECK_LAUNCH("k_axpy");
@@ -819,7 +840,8 @@ static int smooth_post(topt_fem* h, int li, Hier<T>& H, int L, int degree, const
     ep.dold = dA;
     ep.dnew = dB;
     ep.add_old = (k == 1);
-    if ((rc = spmv<T>(h, Ls, h->bs, L, 2, false, vals, dA, nullptr, r, 0, ep))) return rc;
+    if ((rc = spmv<T>(h, Ls, h->bs, L, 2, false, vals, dA, nullptr, r, 0, ep, true)))
+      return rc;
     std::swap(dA, dB);
     rho0 = rho1;
   }
@@ -941,7 +963,9 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
   inf->outer = 0;
   const float* A32 = H.lv[0].vals.as<float>();
   for (int it = 1; it <= maxiter; ++it) {
-    if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5))) return rc;
+    if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5, ChebEp<float>(),
+                          true)))
+      return rc;
     TOPT_L_DISPATCH(L, (k_pcg_update<float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p32, q32,
                            x32, r32, h->red.partials.as<double>(), h->red.ctr(6),
@@ -1030,7 +1054,8 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   *status = TOPT_MAXITER;
   for (it = 1; it <= maxiter; ++it) {
     // q = A p, pq = p.q
-    if ((rc = spmv<T>(h, L0, bs, L, 0, true, vals, p, nullptr, q, 5))) return rc;
+    if ((rc = spmv<T>(h, L0, bs, L, 0, true, vals, p, nullptr, q, 5, ChebEp<T>(), true)))
+      return rc;
     TOPT_L_DISPATCH(L, (k_pcg_update<T, T, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(slot_old), h->red.res(5), active.as<int>(), p, q, x, r,
                            h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6), nullptr)));
@@ -1193,7 +1218,9 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* r64, float* p32, fl
   int it, since = 0;
   for (it = 1; it <= maxiter; ++it) {
     // q32 = A32 p32 and p.q (slot 5); U += a p (FP64), r32 -= a q32, r.r (slot 6)
-    if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5))) return rc;
+    if ((rc = spmv<float>(h, L0, bs, L, 0, true, A32, p32, nullptr, q32, 5, ChebEp<float>(),
+                          true)))
+      return rc;
     TOPT_L_DISPATCH(L, (k_fcg_update32<L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
                            n, h->red.res(3), h->red.res(5), active.as<int>(), p32, q32, U, r32,
                            h->red.partials.as<double>(), h->red.ctr(6), h->red.res(6))));
@@ -1356,13 +1383,12 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
         nm[n] = (uint8_t)((d->dirichlet[3 * n] ? 1 : 0) | (d->dirichlet[3 * n + 1] ? 2 : 0) |
                           (d->dirichlet[3 * n + 2] ? 4 : 0));
       if ((rc = upload(h->nmask, nm.data(), nm.size(), s))) return rc;
+      {
+        std::vector<uint32_t> nm32(nm.begin(), nm.end());
+        if ((rc = upload(h->nmask32, nm32.data(), nm32.size(), s))) return rc;
+      }
       TOPT_CUDA(cudaStreamSynchronize(s));
-      // one grid-reduction partial per tile of the fused p.Ap variant
       h->mf_ty = mf_pick_ty(ny + 1);
-      const int64_t tiles = mf_tiles(h->mfg, h->mf_ty);
-      if (tiles > h->red.max_blocks &&
-          (rc = h->red.init((int)std::min<int64_t>(tiles, INT32_MAX / 8))))
-        return rc;
     }
     if (h->ls.size() > 1) {
       LevelStruct& B = h->ls.back();

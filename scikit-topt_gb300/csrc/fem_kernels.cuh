@@ -365,18 +365,33 @@ __host__ __device__ constexpr int hoff(int a, int d) {
   return d == 0 ? (0xD4 >> a) & 1 : (d == 1 ? (0xB2 >> a) & 1 : (0xE8 >> a) & 1);
 }
 
-// Tiled variant: a CTA of 256 threads owns a TY x 8 x 4 block of nodes (y
-// fastest; TY picked per grid to waste the fewest threads) and each thread
-// computes TY/8 of its nodes.  The CTA stages the node halo -- x as float4
-// per node, fixed DOFs and nodes outside the grid zeroed, the node's fixed
-// flags in .w -- and the coefficients of every cell touching the tile (0
-// outside the grid) in shared memory with row-wise coalesced loads, so the
-// per-node work is branch-free: per cell, 8 LDS.128 of its nodes and 72 FFMA
-// with constant-bank K0 operands.  The MODE 1/2 operand of a node is loaded
-// before its arithmetic.  Two CTAs per SM overlap one tile's staging with the
-// other's arithmetic.  (A Chebyshev step fused here measured slower than a
+// Tiled variant: the grid is persistent (two CTAs of 256 threads per SM) and
+// walks tiles of TY x 8 x 4 nodes (y fastest; TY picked per grid to waste the
+// fewest threads); each thread computes TY/8 nodes of a tile.  A CTA stages
+// the next tile with cp.async while it computes the current one (two
+// buffers): the node halo (x in .xyz, the node's fixed flags in .w; zeros
+// outside the grid), the coefficients of every cell touching the tile (0
+// outside the grid) and, for MODE 1/2, the tile's b or y.  The per-node work
+// is branch-free: per cell, 8 LDS.128 of its nodes and 72 FFMA with
+// constant-bank K0 operands.  COLMASK zeroes the fixed DOFs of x on use
+// (skfem.enforce's zero columns); callers whose x is zero on the fixed DOFs
+// already -- every operand inside the solvers -- skip it.  Fixed rows are
+// identity rows.  (A Chebyshev step fused here measured slower than a
 // separate pass: its loads stall this compute-bound kernel.)
-constexpr int kMfTX = 8, kMfTZ = 4, kMfThreads = 256;
+__device__ __forceinline__ void cp_async4(void* smem, const void* g, bool in) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(sa), "l"(g),
+               "r"(in ? 4 : 0));
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::);
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+constexpr int kMfTX = 8, kMfTZ = 4, kMfThreads = 256, kMfCtasPerSm = 2;
 
 template <int TY>
 struct MfTile {
@@ -384,6 +399,11 @@ struct MfTile {
   static constexpr int CY = TY + 1, CX = kMfTX + 1, CZ = kMfTZ + 1;
   static constexpr int NN = TY * kMfTX * kMfTZ;
   static constexpr int NPT = (NN + kMfThreads - 1) / kMfThreads;
+  static constexpr int XSF = HZ * HX * HY * 4;        // floats of one buffer's parts
+  static constexpr int CSF = (CZ * CX * CY + 3) & ~3;
+  static constexpr int SBF = (NN * 3 + 3) & ~3;
+  static constexpr int BUF = XSF + CSF + SBF;
+  static constexpr int SMEM = 2 * BUF * 4;            // bytes, two buffers
 };
 
 inline int mf_pick_ty(int ny1) {
@@ -396,102 +416,141 @@ inline int mf_pick_ty(int ny1) {
   return best;
 }
 
-inline int64_t mf_tiles(const MfGrid& g, int ty) {
-  return (int64_t)((g.ny + ty) / ty) * ((g.nx + kMfTX) / kMfTX) * ((g.nz + kMfTZ) / kMfTZ);
+template <int TY, int MODE>
+__device__ __forceinline__ void mf_stage(float* buf, int t, const MfGrid& g, int ny1, int nx1,
+                                         int nz1, int nty, int ntx, const float* __restrict__ x,
+                                         const uint32_t* __restrict__ m32,
+                                         const float* __restrict__ coef,
+                                         const float* __restrict__ bsrc) {
+  using G = MfTile<TY>;
+  const int ty = (t % nty) * TY, tx = ((t / nty) % ntx) * kMfTX, tz = (t / (nty * ntx)) * kMfTZ;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float* xs = buf;
+  float* cs = buf + G::XSF;
+  float* sb = cs + G::CSF;
+  for (int row = warp; row < G::HZ * G::HX; row += kMfThreads / 32) {
+    const int hz = row / G::HX, hx = row % G::HX;
+    const int jz = tz - 1 + hz, jx = tx - 1 + hx;
+    const bool rin = jz >= 0 && jz < nz1 && jx >= 0 && jx < nx1;
+    const int base = ny1 * (jx + nx1 * jz);
+    for (int hy = lane; hy < G::HY; hy += 32) {
+      const int jy = ty - 1 + hy;
+      const bool in = rin && jy >= 0 && jy < ny1;
+      const int nb = in ? base + jy : 0;
+      float* d = xs + ((hz * G::HX + hx) * G::HY + hy) * 4;
+      cp_async4(d + 0, x + nb * 3 + 0, in);
+      cp_async4(d + 1, x + nb * 3 + 1, in);
+      cp_async4(d + 2, x + nb * 3 + 2, in);
+      cp_async4(d + 3, m32 + nb, in);
+    }
+  }
+  for (int row = warp; row < G::CZ * G::CX; row += kMfThreads / 32) {
+    const int cz = row / G::CX, cx = row % G::CX;
+    const int ez = tz - 1 + cz, ex = tx - 1 + cx;
+    const bool rin = ez >= 0 && ez < g.nz && ex >= 0 && ex < g.nx;
+    const int base = g.ny * (ex + g.nx * ez);
+    for (int cy = lane; cy < G::CY; cy += 32) {
+      const int ey = ty - 1 + cy;
+      const bool in = rin && ey >= 0 && ey < g.ny;
+      cp_async4(cs + (cz * G::CX + cx) * G::CY + cy, coef + (in ? base + ey : 0), in);
+    }
+  }
+  if (MODE != 0) {
+    for (int row = warp; row < kMfTZ * kMfTX; row += kMfThreads / 32) {
+      const int lz = row / kMfTX, lx = row % kMfTX;
+      const int iz = tz + lz, ix = tx + lx;
+      const bool rin = iz < nz1 && ix < nx1;
+      const int n = min(TY, ny1 - ty) * 3;
+      const int64_t a0 = (int64_t)ty + (int64_t)ny1 * (ix + (int64_t)nx1 * iz);
+      for (int i = lane; i < TY * 3; i += 32) {
+        const bool in = rin && i < n;
+        cp_async4(sb + row * TY * 3 + i, bsrc + (in ? a0 * 3 + i : 0), in);
+      }
+    }
+  }
 }
 
-template <int TY, int MODE, bool DOT>
-__global__ void __launch_bounds__(kMfThreads, 2)
-k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint8_t* __restrict__ nmask,
+template <int TY, int MODE, bool DOT, bool COLMASK>
+__global__ void __launch_bounds__(kMfThreads, kMfCtasPerSm)
+k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint32_t* __restrict__ m32,
           const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
           double* partials, unsigned* counter, double* dot_out) {
   TOPT_KERNEL_COUNT();
   using G = MfTile<TY>;
-  constexpr int TX = kMfTX, TZ = kMfTZ, NT = kMfThreads;
-  constexpr int HY = G::HY, HX = G::HX, HZ = G::HZ, CY = G::CY, CX = G::CX, CZ = G::CZ;
-  __shared__ float4 xs[HZ][HX][HY];
-  __shared__ float cs[CZ][CX][CY];
+  constexpr int TX = kMfTX, TZ = kMfTZ, NT = kMfThreads, HY = G::HY, HX = G::HX;
+  constexpr int CY = G::CY, CX = G::CX;
+  extern __shared__ __align__(16) float smem[];
   const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
-  // 1-D grid of tiles, y tiles fastest (linear block index for the grid reduction)
   const int nty = (ny1 + TY - 1) / TY, ntx = (nx1 + TX - 1) / TX;
-  const int bt = blockIdx.x;
-  const int ty = (bt % nty) * TY, tx = ((bt / nty) % ntx) * TX, tz = (bt / (nty * ntx)) * TZ;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int row = warp; row < HZ * HX; row += NT / 32) {
-    const int hz = row / HX, hx = row % HX;
-    const int jz = tz - 1 + hz, jx = tx - 1 + hx;
-    const bool rin = jz >= 0 && jz < nz1 && jx >= 0 && jx < nx1;
-    const int base = ny1 * (jx + nx1 * jz);
-    for (int hy = lane; hy < HY; hy += 32) {
-      const int jy = ty - 1 + hy;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (rin && jy >= 0 && jy < ny1) {
-        const int nb = base + jy;
-        const int m = nmask ? nmask[nb] : 0;
-        v.x = (m & 1) ? 0.f : x[nb * 3 + 0];
-        v.y = (m & 2) ? 0.f : x[nb * 3 + 1];
-        v.z = (m & 4) ? 0.f : x[nb * 3 + 2];
-        v.w = __int_as_float(m);
-      }
-      xs[hz][hx][hy] = v;
-    }
-  }
-  for (int row = warp; row < CZ * CX; row += NT / 32) {
-    const int cz = row / CX, cx = row % CX;
-    const int ez = tz - 1 + cz, ex = tx - 1 + cx;
-    const bool rin = ez >= 0 && ez < g.nz && ex >= 0 && ex < g.nx;
-    const int base = g.ny * (ex + g.nx * ez);
-    for (int cy = lane; cy < CY; cy += 32) {
-      const int ey = ty - 1 + cy;
-      cs[cz][cx][cy] = (rin && ey >= 0 && ey < g.ny) ? coef[base + ey] : 0.f;
-    }
-  }
-  __syncthreads();
+  const int ntiles = nty * ntx * ((nz1 + TZ - 1) / TZ);
+  const float* bsrc = MODE == 1 ? b : y;
   float tacc = 0.0f;
+  int cur = 0;
+  if ((int)blockIdx.x < ntiles)
+    mf_stage<TY, MODE>(smem, blockIdx.x, g, ny1, nx1, nz1, nty, ntx, x, m32, coef, bsrc);
+  cp_async_commit();
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int tn = t + gridDim.x;
+    if (tn < ntiles)
+      mf_stage<TY, MODE>(smem + (cur ^ 1) * G::BUF, tn, g, ny1, nx1, nz1, nty, ntx, x, m32,
+                         coef, bsrc);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    const float4* xs = reinterpret_cast<const float4*>(smem + cur * G::BUF);
+    const float* cs = smem + cur * G::BUF + G::XSF;
+    const float* sb = cs + G::CSF;
+    const int ty = (t % nty) * TY, tx = ((t / nty) % ntx) * TX, tz = (t / (nty * ntx)) * TZ;
 #pragma unroll 1
-  for (int k = 0; k < G::NPT; ++k) {
-    const int li = threadIdx.x + k * NT;
-    if (li >= G::NN) break;
-    const int ly = li % TY, lx = (li / TY) % TX, lz = li / (TY * TX);
-    const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
-    if (iy >= ny1 || ix >= nx1 || iz >= nz1) continue;
-    const int a = iy + ny1 * (ix + nx1 * iz);
-    float bv[3] = {0.f, 0.f, 0.f};
-    if (MODE != 0) {
-      const float* src = MODE == 1 ? b : y;
+    for (int k = 0; k < G::NPT; ++k) {
+      const int li = threadIdx.x + k * NT;
+      if (li >= G::NN) break;
+      const int ly = li % TY, lx = (li / TY) % TX, lz = li / (TY * TX);
+      const int iy = ty + ly, ix = tx + lx, iz = tz + lz;
+      if (iy >= ny1 || ix >= nx1 || iz >= nz1) continue;
+      float acc[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-      for (int c = 0; c < 3; ++c) bv[c] = src[(int64_t)a * 3 + c];
-    }
-    float acc[3] = {0.0f, 0.0f, 0.0f};
+      for (int la = 0; la < 8; ++la) {
+        float part[3] = {0.0f, 0.0f, 0.0f};
 #pragma unroll
-    for (int la = 0; la < 8; ++la) {
-      float part[3] = {0.0f, 0.0f, 0.0f};
+        for (int lb = 0; lb < 8; ++lb) {
+          const float4 v = xs[((lz + 1 - hoff(la, 2) + hoff(lb, 2)) * HX +
+                               (lx + 1 - hoff(la, 0) + hoff(lb, 0))) * HY +
+                              (ly + 1 - hoff(la, 1) + hoff(lb, 1))];
+          float xv[3] = {v.x, v.y, v.z};
+          if (COLMASK) {
+            const int m = __float_as_int(v.w);
+            xv[0] = (m & 1) ? 0.f : xv[0];
+            xv[1] = (m & 2) ? 0.f : xv[1];
+            xv[2] = (m & 4) ? 0.f : xv[2];
+          }
 #pragma unroll
-      for (int lb = 0; lb < 8; ++lb) {
-        const float4 v = xs[lz + 1 - hoff(la, 2) + hoff(lb, 2)][lx + 1 - hoff(la, 0) + hoff(lb, 0)]
-                           [ly + 1 - hoff(la, 1) + hoff(lb, 1)];
-        const float xv[3] = {v.x, v.y, v.z};
+          for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int c = 0; c < 3; ++c)
+            for (int d = 0; d < 3; ++d)
+              part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
+        }
+        const float s = cs[((lz + 1 - hoff(la, 2)) * CX + (lx + 1 - hoff(la, 0))) * CY +
+                           (ly + 1 - hoff(la, 1))];
 #pragma unroll
-          for (int d = 0; d < 3; ++d)
-            part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
+        for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
       }
-      const float s = cs[lz + 1 - hoff(la, 2)][lx + 1 - hoff(la, 0)][ly + 1 - hoff(la, 1)];
+      const float4 self = xs[((lz + 1) * HX + (lx + 1)) * HY + (ly + 1)];
+      const int ma = __float_as_int(self.w);
+      const int a = iy + ny1 * (ix + nx1 * iz);
+      const float xself[3] = {self.x, self.y, self.z};
 #pragma unroll
-      for (int c = 0; c < 3; ++c) acc[c] = fmaf(s, part[c], acc[c]);
+      for (int c = 0; c < 3; ++c) {
+        const float ax = ((ma >> c) & 1) ? xself[c] : acc[c];
+        const float out = MODE == 0 ? ax : sb[li * 3 + c] - ax;
+        y[(int64_t)a * 3 + c] = out;
+        if (DOT) tacc += xself[c] * out;
+      }
     }
-    // fixed rows act as identity rows (the staged x of a fixed DOF is 0)
-    const int ma = __float_as_int(xs[lz + 1][lx + 1][ly + 1].w);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int64_t idx = (int64_t)a * 3 + c;
-      const float ax = ((ma >> c) & 1) ? x[idx] : acc[c];
-      const float out = MODE == 0 ? ax : bv[c] - ax;
-      y[idx] = out;
-      if (DOT) tacc += x[idx] * out;
-    }
+    __syncthreads();
+    cur ^= 1;
   }
+  cp_async_wait<0>();
   if (DOT) {
     double dacc[1] = {(double)tacc};
     __shared__ double sh[32];
