@@ -123,7 +123,8 @@ __device__ __forceinline__ void block_sum(T (&v)[L], T* sh) {
 }
 
 // Deterministic cross-block finish: every block stores its L partials; the
-// last block to arrive sums them in block order into out[0..L) and re-arms
+// last block to arrive sums them (fixed thread-strided assignment, then the
+// fixed block tree: the same order every call) into out[0..L) and re-arms
 // the counter.  Call from all threads after block_sum (partials in thread 0).
 template <typename T, int L>
 __device__ __forceinline__ bool grid_finish(T (&v)[L], T* partials, unsigned* counter,
@@ -139,24 +140,89 @@ __device__ __forceinline__ bool grid_finish(T (&v)[L], T* partials, unsigned* co
   __syncthreads();
   if (!last) return false;
   __threadfence();
-  // one warp sums the partials: lane-strided partial sums, then a fixed tree
+  // the whole last block sums the partials: thread-strided partial sums (the
+  // L2 loads of a thread are independent and issued back to back), then the
+  // fixed block tree
+  T acc[L];
+#pragma unroll
+  for (int j = 0; j < L; ++j) acc[j] = T(0);
+  const int nb = (int)gridDim.x;
+  int b = threadIdx.x;
+  for (; b + 3 * (int)blockDim.x < nb; b += 4 * blockDim.x) {
+    T v[4][L];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) v[u][j] = __ldcg(partials + (b + u * blockDim.x) * L + j);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) acc[j] += v[u][j];
+  }
+  for (; b < nb; b += blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) acc[j] += __ldcg(partials + b * L + j);
+  }
+  __shared__ T shf[32 * L];
+  block_sum<T, L>(acc, shf);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) out[j] = acc[j];
+    *counter = 0u;
+  }
+  return true;
+}
+
+// Cross-block maximum of non-negative values, NaN-propagating (a NaN in any
+// block gives NaN): call from all threads with the thread's running maximum
+// m and NaN flag; the last block to arrive combines the block maxima with
+// all its threads and writes *out (max is order-free, so the result is
+// deterministic) and re-arms the counter.
+__device__ __forceinline__ void grid_max_finish(double m, bool nan, double* partials,
+                                                unsigned* counter, double* out) {
+  __shared__ double shm[32];
+  __shared__ int anynan;
+  __shared__ bool last;
+  if (threadIdx.x == 0) anynan = 0;
+  __syncthreads();
+  if (nan) anynan = 1;
+  double v = warp_max(m);
+  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
+  __syncthreads();
   if (threadIdx.x < 32) {
-    T acc[L];
-#pragma unroll
-    for (int j = 0; j < L; ++j) acc[j] = T(0);
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
-#pragma unroll
-      for (int j = 0; j < L; ++j) acc[j] += ((volatile T*)partials)[b * L + j];
-    }
-#pragma unroll
-    for (int j = 0; j < L; ++j) acc[j] = warp_sum(acc[j]);
+    double u = threadIdx.x < (int)(blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
+    u = warp_max(u);
     if (threadIdx.x == 0) {
-#pragma unroll
-      for (int j = 0; j < L; ++j) out[j] = acc[j];
+      partials[blockIdx.x] = anynan ? NAN : u;
+      __threadfence();
+      last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double r = 0.0;
+  bool bad = false;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    const double pv = __ldcg(partials + b);
+    if (pv != pv) bad = true;
+    r = pv > r ? pv : r;
+  }
+  __syncthreads();   // shm / anynan reuse
+  if (threadIdx.x == 0) anynan = 0;
+  __syncthreads();
+  if (bad) anynan = 1;
+  v = warp_max(r);
+  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double u = threadIdx.x < (int)(blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
+    u = warp_max(u);
+    if (threadIdx.x == 0) {
+      *out = anynan ? NAN : u;
       *counter = 0u;
     }
   }
-  return true;
 }
 
 }  // namespace topt

@@ -140,31 +140,8 @@ __global__ void k_design_kkt_w(int64_t nd, const int32_t* __restrict__ design,
     const double a = fabs(w[i] * c);
     m = a > m ? a : m;
   }
-  __shared__ double shm[32];
-  __shared__ bool last;
-  double v = warp_max(m);
-  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double u = threadIdx.x < (blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
-    u = warp_max(u);
-    if (threadIdx.x == 0) partials[blockIdx.x] = u;
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double r = 0.0;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      const double pv = ((volatile double*)partials)[b];
-      r = pv > r ? pv : r;
-    }
-    *out = r;
-    *counter = 0u;
-  }
+  // NaN entries never win a comparison here (kept as in the serial maximum)
+  grid_max_finish(m, false, partials, counter, out);
 }
 
 // lagrangian_log_update (logmoc.py:36-66) on the design elements:

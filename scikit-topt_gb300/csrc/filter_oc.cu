@@ -297,38 +297,7 @@ __global__ void k_design_reduce(int64_t nd, const int32_t* __restrict__ design,
     if (a != a) nan = 1;
     m = a > m ? a : m;
   }
-  __shared__ double shm[32];
-  __shared__ int anynan;
-  __shared__ bool last;
-  if (threadIdx.x == 0) anynan = 0;
-  __syncthreads();
-  if (nan) anynan = 1;
-  double v = warp_max(m);
-  if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double u = threadIdx.x < (blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
-    u = warp_max(u);
-    if (threadIdx.x == 0) partials[blockIdx.x] = anynan ? NAN : u;
-  }
-  if (threadIdx.x == 0) {
-    __threadfence();
-    unsigned t = atomicAdd(counter, 1u);
-    last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (last && threadIdx.x == 0) {
-    __threadfence();
-    double r = 0.0;
-    bool bad = false;
-    for (unsigned b = 0; b < gridDim.x; ++b) {
-      const double pv = ((volatile double*)partials)[b];
-      if (pv != pv) bad = true;
-      r = pv > r ? pv : r;
-    }
-    *out = bad ? NAN : r;
-    *counter = 0u;
-  }
+  grid_max_finish(m, nan != 0, partials, counter, out);
 }
 
 __global__ void k_oc_volume(int64_t nd, const int32_t* __restrict__ rowptr,
@@ -468,40 +437,7 @@ __global__ void k_reduce(int64_t n, const double* __restrict__ x, const double* 
     }
   }
   if (OP == 0) {
-    __shared__ double shm[32];
-    __shared__ int anynan;
-    if (threadIdx.x == 0) anynan = 0;
-    __syncthreads();
-    if (nan) anynan = 1;
-    double v = warp_max(acc[0]);
-    if ((threadIdx.x & 31) == 0) shm[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      double u = threadIdx.x < (blockDim.x >> 5) ? shm[threadIdx.x] : 0.0;
-      u = warp_max(u);
-      if (threadIdx.x == 0) {
-        partials[blockIdx.x] = anynan ? NAN : u;
-      }
-    }
-    __shared__ bool last;
-    if (threadIdx.x == 0) {
-      __threadfence();
-      unsigned t = atomicAdd(counter, 1u);
-      last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-      __threadfence();
-      double m = 0.0;
-      bool bad = false;
-      for (unsigned b = 0; b < gridDim.x; ++b) {
-        const double pv = ((volatile double*)partials)[b];
-        if (pv != pv) bad = true;
-        m = pv > m ? pv : m;
-      }
-      *out = bad ? NAN : m;
-      *counter = 0u;
-    }
+    grid_max_finish(acc[0], nan, partials, counter, out);
   } else {
     __shared__ double sh[32];
     block_sum<double, 1>(acc, sh);
