@@ -35,6 +35,8 @@ for _p in (ROOT, os.path.join(ROOT, "scikit-topt_gb300")):
 METRIC = ("OC iters/s at 1.5M hex, mixed-prec vs FP64 GPU "
           "(compliance rel err ≤1e-6)")
 SIZE = (240, 80, 80)
+# DRAM bytes per node of one k_mf_tile launch (ncu, 120x40x40, caches flushed)
+MF_TRAFFIC_PER_NODE = 19.95
 
 
 def parse():
@@ -48,7 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
-    ap.add_argument("--probe", choices=["spmv"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "solve"], default=None,
                     help="profiling target instead of the benchmark")
     return ap.parse_args()
 
@@ -132,7 +134,9 @@ def make_optimizer(size, precision, max_iters, device):
     return opt
 
 
-def timed_run(opt, warmup, steps, sampler=None):
+def timed_run(opt, warmup, steps, sampler=None, label="steps"):
+    """Warm-up, then `steps` OC iterations timed with CUDA events (NVTX range
+    `label`, for profiler filtering)."""
     import torch
     for _ in range(warmup):
         opt.optimize_steps(1)
@@ -144,12 +148,14 @@ def timed_run(opt, warmup, steps, sampler=None):
     if sampler:
         sampler.start()
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push(label)
     e0.record(s)
     t0 = time.perf_counter()
     for _ in range(steps):
         opt.optimize_steps(1)
     e1.record(s)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
     wall = time.perf_counter() - t0
     clocks = sampler.stop() if sampler else None
     l1 = _native.launch_count()
@@ -172,34 +178,41 @@ def _event_time(fn, n=20):
     return e0.elapsed_time(e1) / n * 1e-3
 
 
-def spmv_roofline(opt, peak_gbs):
-    """The dominant kernel of the mixed solve: the FP64 SELL SpMV of the outer
-    flexible CG (one per iteration), timed with CUDA events on the launching
-    stream.  Algorithmic bytes per launch (3x3 BSR, FP64 values, int32 block
-    columns): nnzb*(9*8 + 4) + 4*(n_nodes+1) + 2*8*n_dof.  The FP32 fine-level
-    operator of the inner V-cycle is matrix-free (compute-bound) and reported
-    separately."""
+def roofline(opt, peak_gbs):
+    """Roofline of the kernel with the largest share of the mixed OC iteration:
+    the FP32 matrix-free operator k_mf_tile (four launches per V-cycle plus
+    the search-direction product), timed through the FP32 operator call with
+    CUDA events on the launching stream.  Algorithmic bytes per launch: x and
+    y (2 * 12 B per node), the fixed-DOF flags (4 B per node) and the cell
+    coefficients (4 B per cell).  The kernel is bound by FP32 FMA issue (576
+    FMA per node), not by HBM, so its FLOP rate is reported beside.  The FP64
+    SpMV of the residual replacements is reported as well."""
     import torch
     eng = opt.fem.engine
+    nodes, cells = eng.mesh.nnodes, eng.mesh.nelements
     x64 = torch.rand((eng.n_dof, 1), dtype=torch.float64, device=eng.device)
     x32 = x64.float()
-    t = _event_time(lambda: eng.spmv(x64))
     t32 = _event_time(lambda: eng.spmv(x32, torch.float32))
+    t64 = _event_time(lambda: eng.spmv(x64))
+    bytes_mf = 28 * nodes + 4 * cells
+    # DRAM traffic per launch: an ncu capture of this kernel on the 120x40x40
+    # cantilever (caches flushed) read 4.06 MB and wrote 0 B (the stores
+    # stayed in L2) for 203,401 nodes = MF_TRAFFIC_PER_NODE B per node,
+    # scaled here to this grid's node count.
+    traffic = MF_TRAFFIC_PER_NODE * nodes
     nb = eng.nnzb
-    bytes_alg = nb * (9 * 8 + 4) + 4 * (eng.mesh.nnodes + 1) + 2 * 8 * eng.n_dof
-    achieved = bytes_alg / t / 1e9
-    # DRAM traffic per launch: an ncu capture (dram__bytes_read.sum +
-    # dram__bytes_write.sum) of this kernel on the 120x40x40 cantilever read
-    # and wrote 425.16 MB for 5,285,401 blocks = 80.44 B per block; scaled here
-    # to this launch's block count.
-    traffic = 80.44 * nb
-    mf_flops = 2 * 576 * eng.mesh.nnodes
-    return {"kernel": "k_sell_spmv<double,3,1> (fine-level FP64 SpMV, outer FCG)",
-            "bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
-            "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_alg),
-            "launch_us": round(t * 1e6, 1), "traffic": int(traffic),
-            "fp32_matrix_free_us": round(t32 * 1e6, 1),
-            "fp32_matrix_free_tflops": round(mf_flops / t32 / 1e12, 2)}
+    bytes64 = nb * (9 * 8 + 4) + 4 * (nodes + 1) + 2 * 8 * eng.n_dof
+    achieved = bytes_mf / t32 / 1e9
+    return {"kernel": "k_mf_tile (FP32 matrix-free operator, fine level)", "bound": "hbm",
+            "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+            "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_mf),
+            "launch_us": round(t32 * 1e6, 1), "traffic": int(traffic),
+            "limiter": "FP32 FMA issue",
+            "fp32_tflops": round(2 * 576 * nodes / t32 / 1e12, 2),
+            "fp64_spmv": {"kernel": "k_sell_spmv<double,3,1> (residual replacement)",
+                          "launch_us": round(t64 * 1e6, 1),
+                          "achieved_gbs": round(bytes64 / t64 / 1e9, 1),
+                          "bytes_per_launch": int(bytes64)}}
 
 
 def run_gpu(args):
@@ -216,7 +229,8 @@ def run_gpu(args):
     total = args.warmup + args.steps
     # mixed precision (headline)
     opt = make_optimizer(size, "mixed", max(50, total), dev)
-    ms, wall, launches, clocks = timed_run(opt, args.warmup, args.steps, ClockSampler(local))
+    ms, wall, launches, clocks = timed_run(opt, args.warmup, args.steps, ClockSampler(local),
+                                           label="mixed")
     phases = None
     if args.phases:
         opt.timer.enabled = True
@@ -225,7 +239,7 @@ def run_gpu(args):
         phases = opt.timer.report()
     comp_mixed = list(opt.recorder.histories["compliance"])
     mixed_stats = [(s.iters, s.outer, s.relres) for s in opt.fem.solve_history]
-    roof = spmv_roofline(opt, peak)
+    roof = roofline(opt, peak)
     # same-density check: FP64 solve on the final mixed design
     from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
     f64 = FEM_SimpLinearElasticity(opt.tsk, 1e-9, solver_config=LinearSolverConfig(
@@ -257,7 +271,7 @@ def run_gpu(args):
     fp64 = None
     if not args.no_fp64:
         o64 = make_optimizer(size, "fp64", max(50, total), dev)
-        ms64, wall64, _, _ = timed_run(o64, args.warmup, args.steps)
+        ms64, wall64, _, _ = timed_run(o64, args.warmup, args.steps, label="fp64")
         comp64 = list(o64.recorder.histories["compliance"])
         errs = [abs(a - b) / abs(b) for a, b in zip(comp_mixed, comp64)]
         fp64 = {"value": round(args.steps / (ms64 * 1e-3), 4), "ms_per_step": round(ms64 / args.steps, 2),
@@ -385,8 +399,10 @@ def run_reference(args):
 
 def probe_spmv(size):
     """Profiling target: assemble the mixed engine for a cantilever of `size`
-    and run the level-0 SpMV twice in FP32 (NVTX range "spmv32") and twice in
-    FP64 (range "spmv64")."""
+    and run the level-0 operator twice in FP32 (matrix-free, NVTX range
+    "spmv32") and twice in FP64 (assembled SELL, range "spmv64"), then the
+    FP32 assembled SELL product of an engine without the matrix-free operator
+    twice (range "spmv32sell", the kernel of the coarse levels)."""
     import numpy as np
     import torch
     from sktopt_gb300.fea import composer
@@ -407,14 +423,55 @@ def probe_spmv(size):
             eng.spmv(x, dt)
         torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
+    del eng
+    sell = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True,
+                     matrix_free=False)
+    sell.update(torch.full((tsk.mesh.nelements,), 0.5, dtype=torch.float64, device=dev),
+                1.0, 1e-9, 3.0)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("spmv32sell")
+    for _ in range(2):
+        sell.spmv(x32, torch.float32)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    eng = sell
     print(json.dumps({"probe": "spmv", "size": list(size), "nnzb": eng.nnzb,
                       "n_dof": eng.n_dof}))
+
+
+def probe_solve(size):
+    """Profiling target: one mixed state solve (default scheme) of the
+    cantilever of `size` at a seeded random density, after a warm-up solve,
+    inside the NVTX range "solve"."""
+    import numpy as np
+    import torch
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", 0)
+    tsk = toy_problem.cantilever(*size)
+    fem = FEM_SimpLinearElasticity(tsk, 1e-9, solver_config=LinearSolverConfig(
+        solver="cg_pyamg", rtol=1e-8, precision="mixed"), device=dev)
+    g = np.random.default_rng(0)
+    rho = torch.from_numpy(0.01 + 0.99 * g.random(tsk.mesh.nelements)).to(dev)
+    U = torch.zeros((3 * tsk.mesh.nnodes, 1), dtype=torch.float64, device=dev)
+    fem.solve_device(rho, 3.0, U)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("solve")
+    c = fem.solve_device(rho, 3.0, U)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    st = fem.last_stats
+    print(json.dumps({"probe": "solve", "size": list(size), "compliance": float(c[0]),
+                      "iters": st.iters, "replacements": st.outer, "relres": st.relres}))
 
 
 def main():
     args = parse()
     if args.probe == "spmv":
         probe_spmv(tuple(args.size))
+        return
+    if args.probe == "solve":
+        probe_solve(tuple(args.size))
         return
     if args.impl == "reference":
         run_reference(args)
