@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
-    ap.add_argument("--probe", choices=["spmv", "solve"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "solve", "batch"], default=None,
                     help="profiling target instead of the benchmark")
     return ap.parse_args()
 
@@ -465,6 +465,49 @@ def probe_solve(size):
                       "iters": st.iters, "replacements": st.outer, "relres": st.relres}))
 
 
+def probe_batch(n_designs, iters, workers):
+    """Batched uneven designs: the first `n_designs` cantilevers of the
+    256-design set (seed 0), `iters` mixed OC iterations each, stepped
+    concurrently (one stream per design, `workers` host threads) and then
+    one after another; prints design-iterations per second of both."""
+    import torch
+    from sktopt_gb300 import tools
+    from sktopt_gb300.core import BatchedDesigns, OC_Config, OC_Optimizer
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", 0)
+    specs = toy_problem.batched_cantilever_specs(256, seed=0)[:n_designs]
+
+    def maker(spec):
+        nx, ny, nz, vf, lf = spec
+
+        def make():
+            cfg = OC_Config(max_iters=iters, filter_type="spacial",
+                            filter_radius=tools.SchedulerConfig.constant(target_value=1.5),
+                            p=tools.SchedulerConfig.constant(target_value=3.0),
+                            vol_frac=tools.SchedulerConfig.constant(target_value=vf),
+                            move_limit=tools.SchedulerConfig.constant(target_value=0.2),
+                            E_min_coeff=1e-9, solver_option="cg_pyamg", precision="mixed",
+                            solver_rtol=1e-8)
+            return OC_Optimizer(cfg, toy_problem.cantilever(nx, ny, nz, load_frac=lf),
+                                device=dev)
+        return make
+    out = {"probe": "batch", "designs": n_designs, "iters": iters, "workers": workers,
+           "elements": int(sum(s[0] * s[1] * s[2] for s in specs))}
+    for label, nw in (("concurrent", workers), ("sequential", 1)):
+        batch = BatchedDesigns([maker(s) for s in specs], n_workers=nw, device=dev)
+        batch.step(1)              # warm-up iteration (engines, hierarchies)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batch.step(iters - 1)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[label] = {"design_iters_per_s": round(n_designs * (iters - 1) / dt, 2),
+                      "seconds": round(dt, 3)}
+        del batch
+        torch.cuda.empty_cache()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.probe == "spmv":
@@ -472,6 +515,9 @@ def main():
         return
     if args.probe == "solve":
         probe_solve(tuple(args.size))
+        return
+    if args.probe == "batch":
+        probe_batch(32, 6, 16)
         return
     if args.impl == "reference":
         run_reference(args)

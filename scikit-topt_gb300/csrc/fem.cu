@@ -13,7 +13,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <type_traits>
 #include <vector>
@@ -57,6 +59,7 @@ template <typename T>
 struct Hier {
   std::vector<LevelNum<T>> lv;
   bool built = false;
+  DevBuf dense_scratch;   // FP64 copy of the coarsest operator for its inverse
 };
 
 struct Reducer {
@@ -95,6 +98,7 @@ struct topt_fem {
   topt::Reducer red;
   // PCG / refinement work vectors (n_dof x 8 max loads)
   topt::DevBuf fe, R, U0;
+  topt::DevBuf active;                 // per-load "still iterating" flags (4 ints)
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   bool assembled = false;
@@ -102,6 +106,7 @@ struct topt_fem {
   bool mf = false;
   topt::MfGrid mfg{};
   int mf_ty = 32;                      // y extent of the operator's node tiles
+  float k0_host[576] = {};             // FP32 unit matrix (constant-bank copy)
   topt::DevBuf nmask32;                // nmask widened to 32 bits (cp.async granule)
   topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
 };
@@ -340,7 +345,13 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 // The single-load matrix-free kernel reads K0 from constant memory; the
 // constant bank is per process, so it is (re)loaded on the handle's stream
 // whenever another handle's K0 was loaded last.
-static const void* g_k0_owner = nullptr;
+// The bank is process-wide: handles whose K0 has the same contents share it;
+// a handle with different contents reloads it (under g_k0_mu).  Concurrent
+// handles on different streams must therefore share K0 (uniform grids of the
+// same cell size do); the batched driver checks this.
+static std::mutex g_k0_mu;
+static float g_k0_host[576];
+static int g_k0_dev = -1;
 
 template <int TY, int MODE, bool DOT, bool COLMASK>
 static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y, int slot) {
@@ -370,10 +381,17 @@ template <int L, int MODE, bool DOT>
 static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot,
                      const ChebEp<float>& ep, bool zero_fixed) {
   if (L == 1) {
-    if (g_k0_owner != h->ke32.p) {
-      TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->ke32.p, 576 * sizeof(float), 0,
-                                        cudaMemcpyDeviceToDevice, h->stream));
-      g_k0_owner = h->ke32.p;
+    {
+      std::lock_guard<std::mutex> lk(g_k0_mu);
+      int dev = 0;
+      TOPT_CUDA(cudaGetDevice(&dev));
+      if (g_k0_dev != dev || std::memcmp(g_k0_host, h->k0_host, sizeof(g_k0_host)) != 0) {
+        TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->k0_host, 576 * sizeof(float), 0,
+                                          cudaMemcpyHostToDevice, h->stream));
+        TOPT_CUDA(cudaStreamSynchronize(h->stream));
+        std::memcpy(g_k0_host, h->k0_host, sizeof(g_k0_host));
+        g_k0_dev = dev;
+      }
     }
     const int rc = zero_fixed ? launch_mf_ty<MODE, DOT, false>(h, x, b, y, slot)
                               : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
@@ -688,7 +706,9 @@ template <typename T>
 static int build_dense(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, DevBuf& scratch) {
   const int n = L.ndense;
   int rc;
-  if ((rc = scratch.alloc(sizeof(double) * (size_t)n * n))) return rc;
+  if (scratch.bytes < sizeof(double) * (size_t)n * n &&
+      (rc = scratch.alloc(sizeof(double) * (size_t)n * n)))
+    return rc;
   TOPT_CUDA(cudaMemsetAsync(scratch.p, 0, sizeof(double) * (size_t)n * n, h->stream));
   if (h->bs == 3)
     k_sell_to_dense<T, 3><<<gridsize(h, L.npos), kBlock, 0, h->stream>>>(
@@ -744,7 +764,7 @@ static int refresh(topt_fem* h, Hier<T>& H) {
                            H.lv[0].dinv.template as<T>(), false)))
       return rc;
   }
-  DevBuf scratch;
+  DevBuf& scratch = H.dense_scratch;
   for (int li = 0; li < nlev; ++li) {
     LevelStruct& L = h->ls[li];
     LevelNum<T>& N = H.lv[li];
@@ -948,8 +968,9 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
     rmax[j] = std::sqrt(bn2[j]);
     if (!(bn2[j] > 0.0)) active_h[j] = 0;
   }
-  DevBuf active;
-  if ((rc = upload(active, active_h, 4, h->stream))) return rc;
+  DevBuf& active = h->active;
+  TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
+                            h->stream));
   TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
   TOPT_CUDA(cudaMemsetAsync(x32, 0, sizeof(float) * nl, h->stream));
   k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
@@ -1038,8 +1059,9 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   int active_h[4] = {1, 1, 1, 1};
   for (int j = 0; j < L; ++j)
     if (!(bnorm2[j] > 0.0)) active_h[j] = 0;
-  DevBuf active;
-  if ((rc = upload(active, active_h, 4, h->stream))) return rc;
+  DevBuf& active = h->active;
+  TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
+                            h->stream));
   int slot_old = 3, slot_new = 4;
   auto apply_prec = [&](int slot) -> int {
     return precond_apply<T>(h, H, L, r, z, precond, degree, slot);
@@ -1108,8 +1130,9 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   int active_h[4] = {1, 1, 1, 1};
   for (int j = 0; j < L; ++j)
     if (!(bn2[j] > 0.0)) active_h[j] = 0;
-  DevBuf active;
-  if ((rc = upload(active, active_h, 4, h->stream))) return rc;
+  DevBuf& active = h->active;
+  TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
+                            h->stream));
   TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
   TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice, h->stream));
   k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
@@ -1198,8 +1221,9 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* r64, float* p32, fl
     if (!(bn2[j] > 0.0)) active_h[j] = 0;
     rlast2[j] = bn2[j];
   }
-  DevBuf active;
-  if ((rc = upload(active, active_h, 4, h->stream))) return rc;
+  DevBuf& active = h->active;
+  TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
+                            h->stream));
   TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
   k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
   TOPT_CHECK_LAUNCH("k_convert");
@@ -1320,6 +1344,7 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
     std::vector<float> k32(d->ke, d->ke + nke);
     if ((rc = upload(h->ke32, k32.data(), nke, s))) return rc;
     TOPT_CUDA(cudaStreamSynchronize(s));
+    if (nke == 576) std::copy(k32.begin(), k32.end(), h->k0_host);
   }
   if ((rc = upload(h->mask, d->dirichlet, (size_t)h->n_dof, s))) return rc;
   if ((rc = h->coef64.alloc(sizeof(double) * d->n_elem))) return rc;
@@ -1402,6 +1427,7 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
       }
     }
   }
+  if ((rc = h->active.alloc(4 * sizeof(int)))) return rc;
   if ((rc = h->fe.alloc(sizeof(double) * h->n_dof * 4))) return rc;
   if ((rc = h->R.alloc(sizeof(double) * h->n_dof * 4))) return rc;
   if ((rc = h->U0.alloc(sizeof(double) * h->n_dof * 4 * 4))) return rc;

@@ -445,12 +445,14 @@ __global__ void k_reduce(int64_t n, const double* __restrict__ x, const double* 
   }
 }
 
-// static scratch for the stand-alone reductions (one set per process/device)
+// scratch of the stand-alone reductions (one set per host thread and device)
 struct ReduceScratch {
   DevBuf partials, counter, out;
   int dev = -1;
 };
-static ReduceScratch g_red;
+// per host thread: calls from different threads (on different streams) never
+// share it
+static thread_local ReduceScratch g_red;
 
 static int reduce_scratch(int blocks) {
   int dev = 0;

@@ -64,3 +64,21 @@ def multi_load_tet(nx=160, ny=80, nz=40, lx=2.0, ly=1.0, lz=1.0, jitter=0.2, see
         nodes.append(np.array([node]))
     return LinearElasticity.from_nodes(mesh, dn, "all", nodes, loads,
                                        np.arange(mesh.nelements), E, nu)
+
+
+def batched_cantilever_specs(n=256, seed=0):
+    """The batched-designs configuration: n cantilevers with nx ~ U{16..64},
+    ny, nz ~ U{8..32}, volume fraction ~ U(0.2, 0.5) and the load at a
+    position ~ U(0, 1) along the x = L bottom edge (snapped to the nearest
+    node), all from one seeded generator.  Returns (nx, ny, nz, vf, load_frac)
+    tuples."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        nx = int(rng.integers(16, 65))
+        ny = int(rng.integers(8, 33))
+        nz = int(rng.integers(8, 33))
+        vf = float(rng.uniform(0.2, 0.5))
+        lf = float(rng.uniform(0.0, 1.0))
+        out.append((nx, ny, nz, vf, lf))
+    return out
