@@ -102,6 +102,11 @@ int topt_fem_sizes(const topt_fem* h, int64_t* n_dof, int64_t* nnzb,
  * then the preconditioner refreshed.  rho: dev, n_elem doubles. */
 int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin,
                     double p);
+/* Material interpolation of the later topt_fem_update / topt_fem_energy calls:
+ * kind 0 SIMP (default; composer.py:19-22, dC_drho_simp derivatives.py:25-52),
+ * 1 RAMP E = Emin + (E0 - Emin) rho / (1 + p (1 - rho)) (composer.py:25-39,
+ * dC_drho_ramp derivatives.py:56-72), p being the RAMP parameter. */
+int topt_fem_set_interpolation(topt_fem* h, int32_t kind);
 
 typedef struct topt_solve_opts {
   int32_t method;         /* 0: FP64 PCG.  Mixed (FP32 operator, hierarchy and

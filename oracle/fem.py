@@ -32,6 +32,16 @@ def simp_interpolation(rho, E0, Emin, p):
     return Emin + (E0 - Emin) * (rho ** p)
 
 
+def ramp_interpolation(rho, E0, Emin, p):
+    """composer.py:25-39: Emin + (E0 - Emin) rho / (1 + p (1 - rho))."""
+    return Emin + (E0 - Emin) * (rho / (1.0 + p * (1.0 - rho)))
+
+
+def material(kind):
+    """E(rho) of the interpolation named in DensityMethodConfig.interpolation."""
+    return {"SIMP": simp_interpolation, "RAMP": ramp_interpolation}[kind]
+
+
 def lame(E, nu):
     """composer.py:82-83."""
     lam = (nu * E) / ((1.0 + nu) * (1.0 - 2.0 * nu))
@@ -244,6 +254,19 @@ def dC_drho_simp(rho, strain_energy, E0, Emin, p):
     return -2.0 * strain_energy * dE / np.maximum(E, 1e-12)
 
 
+def dC_drho_ramp(rho, strain_energy, E0, Emin, p):
+    """derivatives.py:56-72 (dE_drho_ramp, _E_ramp)."""
+    den = 1.0 + p * (1.0 - rho)
+    dE = (E0 - Emin) * (den - p * rho) / (den ** 2)
+    E = Emin + (E0 - Emin) * (rho / den)
+    return -2.0 * strain_energy * dE / np.maximum(E, 1e-12)
+
+
+def sensitivity(kind):
+    """dC/drho of the interpolation named in DensityMethodConfig.interpolation."""
+    return {"SIMP": dC_drho_simp, "RAMP": dC_drho_ramp}[kind]
+
+
 class ElasticProblem:
     """Linear elasticity on a GridMesh with nodal loads (task_elastic.py:85-147)."""
 
@@ -268,7 +291,7 @@ class ElasticProblem:
         self.dofs = element_dofs(mesh.t, 3)
 
     def stiffness(self, rho, p, Emin):
-        E = simp_interpolation(rho, self.E0, Emin, p)
+        E = material(getattr(self, "interp", "SIMP"))(rho, self.E0, Emin, p)
         return assemble(self.mesh.t, self.Kloc, E, self.mesh.nnodes, 3)
 
     def objectives(self, rho, p, Emin, solver="spsolve", rtol=1e-8,
@@ -288,7 +311,7 @@ class ElasticProblem:
 
     def energy(self, rho, p, Emin, U):
         """strain_energy_skfem_multi solver_elastic.py:507-537."""
-        E = simp_interpolation(rho, self.E0, Emin, p)
+        E = material(getattr(self, "interp", "SIMP"))(rho, self.E0, Emin, p)
         out = np.empty((rho.size, U.shape[1]))
         for i in range(U.shape[1]):
             out[:, i] = 0.5 * E * element_quadratic(U[:, i], self.dofs, self.Kloc)

@@ -114,6 +114,7 @@ class OracleConfig:
     lagrangian_scale_floor: float = 1e-8
     dual_update: str = "ema"
     solver: str = "spsolve"
+    interpolation: str = "SIMP"        # "SIMP" | "RAMP" (common_density.py:392-404)
     rtol: float = 1e-8
 
 
@@ -165,6 +166,7 @@ class OracleOptimizer:
         rho_f = self.filt.forward(self.rho)
         rho_p = heaviside_projection(rho_f, beta, cfg.beta_eta)
         Emin = self.pb.E0 * cfg.E_min_coeff
+        self.pb.interp = cfg.interpolation
         if isinstance(self.pb, fem.ElasticProblem):
             comp, U = self.pb.objectives(rho_p, p, Emin, cfg.solver, cfg.rtol,
                                          force_scale=nscale)
@@ -174,7 +176,7 @@ class OracleOptimizer:
         dH = heaviside_projection_derivative(rho_f, beta, cfg.beta_eta)
         dC_full = np.zeros_like(self.rho)
         for i in range(U.shape[1]):
-            dCp = fem.dC_drho_simp(rho_p, energy[:, i], self.pb.E0, Emin, p)
+            dCp = fem.sensitivity(cfg.interpolation)(rho_p, energy[:, i], self.pb.E0, Emin, p)
             dC_full += self.filt.gradient(dCp * dH)
         dC_full /= U.shape[1]
         dC_d = dC_full[self.design].copy()

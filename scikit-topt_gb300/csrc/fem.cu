@@ -101,6 +101,7 @@ struct topt_fem {
   topt::DevBuf active;                 // per-load "still iterating" flags (4 ints)
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
+  int interp = 0;                      // 0 SIMP, 1 RAMP
   bool assembled = false;
   // matrix-free FP32 level-0 operator (uniform hex grid, shared unit matrix)
   bool mf = false;
@@ -1456,11 +1457,20 @@ int topt_fem_sizes(const topt_fem* h, int64_t* n_dof, int64_t* nnzb, int32_t* n_
   return TOPT_OK;
 }
 
+int topt_fem_set_interpolation(topt_fem* h, int32_t kind) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_interpolation: null handle");
+  if (kind != 0 && kind != 1)
+    return fail(TOPT_BAD_INPUT, "fem_set_interpolation: kind must be 0 (SIMP) or 1 (RAMP)");
+  h->interp = kind;
+  return TOPT_OK;
+}
+
 int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin, double p) {
   if (!h || !rho) return fail(TOPT_BAD_INPUT, "fem_update: null argument");
   h->E0 = E0; h->Emin = Emin; h->p = p;
   k_simp_coef<<<gridsize(h, h->n_elem), kBlock, 0, h->stream>>>(
-      h->n_elem, rho, E0, Emin, p, h->coef64.as<double>(), h->mixed ? h->coef32.as<float>() : nullptr);
+      h->n_elem, rho, E0, Emin, p, h->coef64.as<double>(),
+      h->mixed ? h->coef32.as<float>() : nullptr, h->interp);
   TOPT_CHECK_LAUNCH("k_simp_coef");
   int rc;
   if (h->mixed) {
@@ -1632,16 +1642,16 @@ int topt_fem_energy(topt_fem* h, const double* U, int32_t nrhs, const double* rh
   const double* ke = h->ke64.as<double>();
   if (h->bs == 3 && h->nloc == 8)
     k_energy<3, 8><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc);
+                                              p, dh, energy, dc, h->interp);
   else if (h->bs == 3)
     k_energy<3, 4><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc);
+                                              p, dh, energy, dc, h->interp);
   else if (h->nloc == 8)
     k_energy<1, 8><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc);
+                                              p, dh, energy, dc, h->interp);
   else
     k_energy<1, 4><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc);
+                                              p, dh, energy, dc, h->interp);
   TOPT_CHECK_LAUNCH("k_energy");
   return TOPT_OK;
 }

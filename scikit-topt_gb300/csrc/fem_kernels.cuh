@@ -11,15 +11,23 @@
 namespace topt {
 
 // --------------------------------------------------------------------------
-// SIMP coefficient E(rho) = Emin + (E0 - Emin) rho^p  (composer.py:19-22)
+// Material interpolation E(rho): interp 0 SIMP, Emin + (E0 - Emin) rho^p
+// (composer.py:19-22); 1 RAMP, Emin + (E0 - Emin) rho / (1 + p (1 - rho))
+// (composer.py:25-39).
+__device__ __forceinline__ double interp_E(int interp, double r, double E0, double Emin,
+                                           double p) {
+  if (interp == 1) return Emin + (E0 - Emin) * (r / (1.0 + p * (1.0 - r)));
+  return Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
+}
+
 __global__ void k_simp_coef(int64_t n, const double* __restrict__ rho, double E0,
                             double Emin, double p, double* __restrict__ c64,
-                            float* __restrict__ c32) {
+                            float* __restrict__ c32, int interp) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double r = rho[i];
-    const double v = Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
+    const double v = interp_E(interp, r, E0, Emin, p);
     if (c64) c64[i] = v;
     if (c32) c32[i] = (float)v;
   }
@@ -1440,7 +1448,7 @@ __global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
                          const double* __restrict__ ke, int64_t ke_stride,
                          const double* __restrict__ U, const double* __restrict__ rho,
                          double E0, double Emin, double p, const double* __restrict__ dh,
-                         double* __restrict__ energy, double* __restrict__ dc) {
+                         double* __restrict__ energy, double* __restrict__ dc, int interp) {
   TOPT_KERNEL_COUNT();
   constexpr int ND = BS * NLOC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1456,11 +1464,18 @@ __global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
 #pragma unroll
     for (int a = 0; a < NLOC; ++a) node[a] = t[(int64_t)a * ne + e];
     const double r = rho[e];
-    const double coef = Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
-    const double rc = fmax(r, 1e-6);
-    const double rp1 = (p == 3.0) ? rc * rc : pow(rc, p - 1.0);
-    const double dE = p * (E0 - Emin) * rp1;
-    const double Ec = fmax(Emin + (E0 - Emin) * rp1 * rc, 1e-12);
+    const double coef = interp_E(interp, r, E0, Emin, p);
+    double dE, Ec;
+    if (interp == 1) {   // dC_drho_ramp (derivatives.py:56-72)
+      const double den = 1.0 + p * (1.0 - r);
+      dE = (E0 - Emin) * (den - p * r) / (den * den);
+      Ec = fmax(coef, 1e-12);
+    } else {             // dC_drho_simp (derivatives.py:25-52), rho clamped at 1e-6
+      const double rc = fmax(r, 1e-6);
+      const double rp1 = (p == 3.0) ? rc * rc : pow(rc, p - 1.0);
+      dE = p * (E0 - Emin) * rp1;
+      Ec = fmax(Emin + (E0 - Emin) * rp1 * rc, 1e-12);
+    }
     const double h = dh ? dh[e] : 1.0;
     for (int j = 0; j < L; ++j) {
       double u[ND];

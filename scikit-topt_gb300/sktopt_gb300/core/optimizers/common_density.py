@@ -22,6 +22,7 @@ import torch
 
 from ... import tools
 from ..._device import default_device
+from ...fea import composer
 from ...fea.solver_elastic import (FEM_SimpLinearElasticity, LinearSolverConfig,
                                    normalize_linear_solver_config)
 from ...filters.spacial import SpacialFilter
@@ -131,8 +132,8 @@ class DensityMethod_OC_Config(DensityMethodConfig):
 
 class DensityMethod:
     def __init__(self, cfg: DensityMethodConfig, tsk, device=None):
-        if cfg.interpolation != "SIMP":
-            raise NotImplementedError("the GPU path implements SIMP interpolation only")
+        if cfg.interpolation not in ("SIMP", "RAMP"):
+            raise ValueError("Interpolation method must be SIMP or RAMP.")
         if cfg.scaling:
             raise NotImplementedError("length/force scaling is not supported")
         self.cfg = cfg
@@ -144,13 +145,18 @@ class DensityMethod:
             cfg.export_cfg(cfg.dst_path)
         if cfg.design_dirichlet is False:
             tsk.exlude_dirichlet_from_design()
+        # common_density.py:392-404 (interpolation_funcs)
+        interp = composer.ramp_interpolation if cfg.interpolation == "RAMP" else \
+            composer.simp_interpolation
         if isinstance(tsk, LinearElasticity):
             self.fem = FEM_SimpLinearElasticity(tsk, cfg.E_min_coeff,
+                                                density_interpolation=interp,
                                                 solver_config=cfg.solver_config,
                                                 device=self.device)
         elif isinstance(tsk, LinearHeatConduction):
             from ...fea.solver_heat import FEM_SimpLinearHeatConduction
             self.fem = FEM_SimpLinearHeatConduction(tsk, cfg.E_min_coeff,
+                                                    density_interpolation=interp,
                                                     solver_config=cfg.solver_config,
                                                     device=self.device)
         else:

@@ -1,6 +1,6 @@
 """Element matrices and material interpolation (set-up, host side).
 
-Mirrors sktopt/fea/composer.py: SIMP interpolation (19-22), Lame parameters
+Mirrors sktopt/fea/composer.py: SIMP and RAMP interpolation (19-39), Lame parameters
 (82-83), and the bilinear forms assembled by ``assemble_stiffness_matrix``
 (53-101: lambda tr(eps(u)) tr(eps(v)) + 2 mu eps(u):eps(v)) and
 ``assemble_conduction_matrix`` (104-145: grad u . grad v) for the
@@ -18,6 +18,21 @@ from ..mesh.grid import HEX_OFFSETS, GridMesh
 def simp_interpolation(rho, E0, Emin, p):
     """composer.py:19-22."""
     return Emin + (E0 - Emin) * (rho ** p)
+
+
+def ramp_interpolation(rho, E0, Emin, p):
+    """composer.py:25-39: Emin + (E0 - Emin) rho / (1 + p (1 - rho))."""
+    return Emin + (E0 - Emin) * (rho / (1.0 + p * (1.0 - rho)))
+
+
+def interpolation_kind(fn) -> int:
+    """Kernel code of a material interpolation: 0 SIMP, 1 RAMP."""
+    name = getattr(fn, "__name__", "")
+    if fn is simp_interpolation or name == "simp_interpolation":
+        return 0
+    if fn is ramp_interpolation or name == "ramp_interpolation":
+        return 1
+    raise NotImplementedError("the GPU path implements SIMP and RAMP interpolation")
 
 
 def lame_parameters(E, nu):

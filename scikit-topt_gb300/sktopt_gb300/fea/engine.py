@@ -91,6 +91,10 @@ class FemEngine:
     def _bind(self):
         N.check(self.lib.topt_fem_set_stream(self.h, C.c_void_p(stream_handle())))
 
+    def set_interpolation(self, kind: int):
+        """0 SIMP, 1 RAMP for the later update / energy calls."""
+        N.check(self.lib.topt_fem_set_interpolation(self.h, int(kind)))
+
     def update(self, rho: torch.Tensor, E0: float, Emin: float, p: float):
         """coef = SIMP(rho); K = sum coef Ke; enforce; refresh the preconditioner."""
         self._bind()

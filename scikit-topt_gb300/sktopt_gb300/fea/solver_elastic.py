@@ -90,16 +90,14 @@ def normalize_linear_solver_config(solver="spsolve", rtol=1e-8, maxiter=None,
 
 
 class FEM_SimpLinearElasticity:
-    """GPU state solve, compliance, energies and sensitivities (SIMP only)."""
+    """GPU state solve, compliance, energies and sensitivities (SIMP or RAMP)."""
 
     def __init__(self, task, E_min_coeff: float,
                  density_interpolation: Callable = composer.simp_interpolation,
                  solver_config: LinearSolverConfig | None = None,
                  solver_option: SolverSelector = "spsolve", petsc_options=None,
                  device=None):
-        if density_interpolation is not composer.simp_interpolation and \
-                getattr(density_interpolation, "__name__", "") != "simp_interpolation":
-            raise NotImplementedError("the GPU path implements SIMP interpolation only")
+        self.interp_kind = composer.interpolation_kind(density_interpolation)
         self.task = task
         self.E_max = task.E * 1.0
         self.E_min = task.E * E_min_coeff
@@ -128,6 +126,7 @@ class FEM_SimpLinearElasticity:
                 multigrid=(cfg.resolved_precond() == "mg"),
                 mg_levels=cfg.mg_levels, mg_coarse_max=cfg.mg_coarse_max,
                 device=self.device)
+            self._engine.set_interpolation(self.interp_kind)
             F = np.column_stack(self.task.neumann_linear)
             self._F = torch.from_numpy(np.ascontiguousarray(F)).to(self.device)
         return self._engine

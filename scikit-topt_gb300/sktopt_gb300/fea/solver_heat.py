@@ -36,8 +36,7 @@ class FEM_SimpLinearHeatConduction:
                  density_interpolation: Callable = composer.simp_interpolation,
                  solver_config: LinearSolverConfig | None = None,
                  solver_option: str = "spsolve", q: int = 4, device=None):
-        if getattr(density_interpolation, "__name__", "") != "simp_interpolation":
-            raise NotImplementedError("the GPU path implements SIMP interpolation only")
+        self.interp_kind = composer.interpolation_kind(density_interpolation)
         if getattr(task, "objective", "compliance") != "compliance":
             raise NotImplementedError("the GPU heat path implements the compliance objective")
         if float(getattr(task, "dirichlet_values", 0.0)) != 0.0:
@@ -67,6 +66,7 @@ class FEM_SimpLinearHeatConduction:
                                      multigrid=(cfg.resolved_precond() == "mg"),
                                      mg_levels=cfg.mg_levels, mg_coarse_max=cfg.mg_coarse_max,
                                      device=self.device)
+            self._engine.set_interpolation(self.interp_kind)
             self._F = torch.from_numpy(np.ascontiguousarray(self.task.emit)[:, None]).to(
                 self.device)
         return self._engine

@@ -127,3 +127,59 @@ def test_filtered_compliance_gradient_matches_oracle_chain(native_lib):
     assert abs(float(C.detach()) - comp[0]) <= 1e-10 * abs(comp[0])
     gr = x.grad.cpu().numpy()
     assert np.linalg.norm(gr - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def test_ramp_interpolation_matches_oracle(native_lib):
+    """RAMP (composer.py:25-39, derivatives.py:56-72): assembled operator,
+    compliance, energies and sensitivities against the oracle, and a short
+    OC loop with interpolation="RAMP" against the oracle loop."""
+    import torch
+    from sktopt_gb300 import tools
+    from sktopt_gb300.core import OC_Config, OC_Optimizer
+    from sktopt_gb300.fea import composer
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.mesh import toy_problem
+    from oracle import optim as oopt
+    dev = torch.device("cuda", 0)
+    nx, ny, nz = 10, 5, 4
+    tsk = toy_problem.cantilever(nx, ny, nz)
+    m, pb, design, fixed, vol = problems.cantilever(nx, ny, nz)
+    pb.interp = "RAMP"
+    rho = np.random.default_rng(21).uniform(0.05, 1.0, tsk.mesh.nelements)
+    q = 3.0
+    comp_ref, U_ref = pb.objectives(rho, q, 1e-9, "spsolve")
+    en_ref = pb.energy(rho, q, 1e-9, U_ref)
+    dc_ref = ofem.dC_drho_ramp(rho, en_ref[:, 0], 1.0, 1e-9, q)
+    fem = FEM_SimpLinearElasticity(tsk, 1e-9, density_interpolation=composer.ramp_interpolation,
+                                   solver_config=LinearSolverConfig(solver="cg_pyamg", rtol=1e-12),
+                                   device=dev)
+    U = torch.zeros((3 * tsk.mesh.nnodes, 1), dtype=torch.float64, device=dev)
+    rt = torch.from_numpy(rho).to(dev)
+    comp = fem.solve_device(rt, q, U)
+    assert abs(comp[0] - comp_ref[0]) <= 1e-10 * abs(comp_ref[0])
+    en, dc = fem.engine.energy(U, rt, 1.0, 1e-9, q, want_dc=True)
+    assert np.linalg.norm(en.cpu().numpy() - en_ref) <= 1e-9 * np.linalg.norm(en_ref)
+    assert np.linalg.norm(dc.cpu().numpy()[:, 0] - dc_ref) <= 1e-9 * np.linalg.norm(dc_ref)
+    # short OC loop
+    n_iter = 4
+    cfg = OC_Config(max_iters=n_iter, filter_type="spacial", interpolation="RAMP",
+                    filter_radius=tools.SchedulerConfig.constant(target_value=1.5),
+                    p=tools.SchedulerConfig.constant(target_value=q),
+                    vol_frac=tools.SchedulerConfig.constant(target_value=0.3),
+                    move_limit=tools.SchedulerConfig.constant(target_value=0.2),
+                    E_min_coeff=1e-9, solver_option="spsolve")
+    opt = OC_Optimizer(cfg, toy_problem.cantilever(nx, ny, nz), device=dev)
+    opt.parameterize()
+    ocfg = oopt.OracleConfig(method="oc", max_iters=n_iter, p=oopt.Sched("Constant", q, q),
+                             vol_frac=oopt.Sched("Constant", 0.3, 0.3),
+                             move_limit=oopt.Sched("Constant", 0.2, 0.2),
+                             filter_radius=oopt.Sched("Constant", 1.5, 1.5),
+                             E_min_coeff=1e-9, interpolation="RAMP")
+    filt = problems.gaussian_filter_for(m, design, 1.5)
+    ref = oopt.OracleOptimizer(ocfg, pb, filt, design, fixed, vol)
+    for k in range(n_iter):
+        opt.optimize_steps(1)
+        c_ref = ref.step()
+        c = opt.recorder.histories["compliance"][-1]
+        assert abs(c - c_ref) <= 1e-9 * abs(c_ref), (k, c, c_ref)
+        np.testing.assert_allclose(opt._state.rho.cpu().numpy(), ref.rho, rtol=0, atol=1e-7)
