@@ -251,22 +251,29 @@ def run_gpu(args):
     c32 = float(opt.fem.solve_device(st.rho_projected, 3.0, U32)[0])
     same_density_err = abs(c32 - c64) / abs(c64)
     del f64
-    # e2e: host-buffer call path
+    n = opt.tsk.mesh.nelements
+    del opt
+    torch.cuda.empty_cache()
+    # e2e: the same iterations (same start, same warm-up) through the
+    # host-buffer call path: density from pinned host memory in, density and
+    # compliance back out, every step
     e2e = None
     if not args.no_e2e:
-        opt.fem._engine  # keep the engine
-        rho_h = torch.empty(opt.tsk.mesh.nelements, dtype=torch.float64).pin_memory()
-        rho_h.copy_(st.rho)
+        oe = make_optimizer(size, "mixed", max(50, total), dev)
+        rho_h = torch.empty(n, dtype=torch.float64).pin_memory()
+        oe.optimize_steps(1)                  # state initialised
+        rho_h.copy_(oe._state.rho)
+        for _ in range(args.warmup - 1):
+            oe.step_host(rho_h)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            opt.step_host(rho_h)
+            oe.step_host(rho_h)
         e2e_wall = time.perf_counter() - t0
-        n = opt.tsk.mesh.nelements
         e2e = {"value": round(args.steps / e2e_wall * world, 4), "unit": "OC iters/s",
                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8}
-    del opt
-    torch.cuda.empty_cache()
+        del oe
+        torch.cuda.empty_cache()
     # plain FP64 run from the same start
     fp64 = None
     if not args.no_fp64:

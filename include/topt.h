@@ -126,6 +126,7 @@ typedef struct topt_solve_opts {
                              iterations between residual replacements       */
   int32_t cheb_degree;    /* Chebyshev smoother degree                       */
   int32_t check_every;    /* residual check period (iterations)              */
+  double cheb_ratio;      /* Chebyshev interval [lmax/ratio, lmax] (0: 30)   */
 } topt_solve_opts;
 
 typedef struct topt_solve_info {

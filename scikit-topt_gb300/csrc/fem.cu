@@ -102,6 +102,7 @@ struct topt_fem {
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   int interp = 0;                      // 0 SIMP, 1 RAMP
+  double cheb_ratio = 30.0;            // smoother interval [lmax/ratio, lmax]
   bool assembled = false;
   // matrix-free FP32 level-0 operator (uniform hex grid, shared unit matrix)
   bool mf = false;
@@ -398,9 +399,9 @@ static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int 
                               : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
     if (rc) return rc;
     if (ep.kind) {
-      k_cheb_step<float, 3, 1><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(h->n_nodes,
-                                                                                 ep, y);
-      TOPT_CHECK_LAUNCH("k_cheb_step");
+      k_cheb_mf<<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
+          h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, y);
+      TOPT_CHECK_LAUNCH("k_cheb_mf");
     }
     return TOPT_OK;
   }
@@ -726,11 +727,11 @@ static int build_dense(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, DevBuf
 }
 
 // Chebyshev smoothing (Saad, Iterative Methods, Alg. 12.1) on the interval
-// [lmax/30, lmax] of Dinv A.
+// [lmax/ratio, lmax] of Dinv A (ratio 30 by default).
 struct ChebParams {
   double theta, delta, sigma;
-  explicit ChebParams(double lmax) {
-    const double lmin = lmax / 30.0;
+  ChebParams(double lmax, double ratio) {
+    const double lmin = lmax / ratio;
     theta = 0.5 * (lmax + lmin);
     delta = 0.5 * (lmax - lmin);
     sigma = theta / delta;
@@ -752,7 +753,7 @@ static int refresh(topt_fem* h, Hier<T>& H) {
   const int64_t stride0 = h->n_ke == 1 ? 0 : (int64_t)(bs * h->nloc) * (bs * h->nloc);
   // level 0 operator (FP32 of a uniform hex grid: matrix-free, diagonal only)
   if (std::is_same<T, float>::value && h->mf) {
-    k_mf_diag_inv<float><<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
+    k_mf_diag_inv<<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
         h->mfg, h->ke32.as<float>(), h->coef32.as<float>(), h->mask.as<uint8_t>(),
         (float*)H.lv[0].dinv.p);
     TOPT_CHECK_LAUNCH("k_mf_diag_inv");
@@ -800,7 +801,7 @@ template <typename T>
 static int smooth_pre(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b, T* x) {
   LevelStruct& Ls = h->ls[li];
   LevelNum<T>& N = H.lv[li];
-  const ChebParams cp(N.lmax);
+  const ChebParams cp(N.lmax, h->cheb_ratio);
   double rho0 = 1.0 / cp.sigma;
   T* r = N.r.template as<T>();
   T* dA = N.d.template as<T>();
@@ -833,7 +834,7 @@ template <typename T>
 static int smooth_post(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b, T* x) {
   LevelStruct& Ls = h->ls[li];
   LevelNum<T>& N = H.lv[li];
-  const ChebParams cp(N.lmax);
+  const ChebParams cp(N.lmax, h->cheb_ratio);
   double rho0 = 1.0 / cp.sigma;
   T* r = N.r.template as<T>();
   T* dA = N.d.template as<T>();
@@ -887,18 +888,30 @@ static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b
     return TOPT_OK;
   }
   if (!started) {
-    const ChebParams cp(N.lmax);
-    TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
-                                                  h->stream>>>(
-                                 Ls.n_nodes, N.dinv.template as<T>(), b, N.d.template as<T>(),
-                                 x, T(0), (T)(1.0 / cp.theta), 1, 1)));
-    TOPT_CHECK_LAUNCH("k_cheb");
+    const ChebParams cp(N.lmax, h->cheb_ratio);
+    if (std::is_same<T, float>::value && h->mf && li == 0 && L == 1) {
+      // first step d = x = Dinv b / theta with the diagonal recomputed
+      ChebEp<float> ep;
+      ep.kind = 3;
+      ep.c2 = (float)(1.0 / cp.theta);
+      ep.dnew = (float*)N.d.p;
+      ep.x = (float*)x;
+      k_cheb_mf<<<gridsize(h, Ls.n_nodes), kBlock, 0, h->stream>>>(
+          h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, (const float*)b);
+      TOPT_CHECK_LAUNCH("k_cheb_mf");
+    } else {
+      TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
+                                                    h->stream>>>(
+                                   Ls.n_nodes, N.dinv.template as<T>(), b, N.d.template as<T>(),
+                                   x, T(0), (T)(1.0 / cp.theta), 1, 1)));
+      TOPT_CHECK_LAUNCH("k_cheb");
+    }
   }
   if ((rc = smooth_pre<T>(h, li, H, L, degree, b, x))) return rc;
   LevelNum<T>& C = H.lv[li + 1];
   const LevelStruct& Cs = h->ls[li + 1];
   const uint8_t* mask = li == 0 ? h->mask.as<uint8_t>() : nullptr;
-  const T c2c = Cs.dense ? T(0) : (T)(1.0 / ChebParams(C.lmax).theta);
+  const T c2c = Cs.dense ? T(0) : (T)(1.0 / ChebParams(C.lmax, h->cheb_ratio).theta);
   const T* dinv_c = Cs.dense ? nullptr : C.dinv.template as<T>();
   TOPT_BSL_DISPATCH(bs, L, (k_restrict<T, BS_, L_><<<gridsize(h, Cs.n_nodes), kBlock, 0,
                                                      h->stream>>>(
@@ -1541,6 +1554,7 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
   const int64_t n = h->n_dof, nl = n * L;
   const int check = o->check_every > 0 ? o->check_every : 1;
   const int degree = o->cheb_degree > 0 ? o->cheb_degree : 2;
+  h->cheb_ratio = o->cheb_ratio > 1.0 ? o->cheb_ratio : 30.0;
   int rc;
   topt_solve_info inf{};
   k_enforce_rhs<<<gridsize(h, nl), kBlock, 0, h->stream>>>(n, L, h->mask.as<uint8_t>(), F,

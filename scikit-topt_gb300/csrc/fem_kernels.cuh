@@ -181,12 +181,11 @@ struct ChebEp {
   int kind = 0, add_old = 0;
 };
 
+// The update of one block row given its inverted diagonal block Dv.  kind 3
+// (first step from a zero guess): dn = c2 Dinv r, x = dn.
 template <typename T, int BS, int L>
-__device__ __forceinline__ void cheb_epilogue(const ChebEp<T>& ep, int64_t row, const T* r) {
-  const T* D = ep.dinv + row * BS * BS;
-  T Dv[BS * BS];
-#pragma unroll
-  for (int q = 0; q < BS * BS; ++q) Dv[q] = D[q];
+__device__ __forceinline__ void cheb_update(const ChebEp<T>& ep, int64_t row, const T* r,
+                                            const T* Dv) {
 #pragma unroll
   for (int c = 0; c < BS; ++c)
 #pragma unroll
@@ -197,6 +196,10 @@ __device__ __forceinline__ void cheb_epilogue(const ChebEp<T>& ep, int64_t row, 
       const int64_t idx = row * BS * L + c * L + j;
       if (ep.kind == 1) {
         ep.dnew[idx] = ep.c2 * s;
+      } else if (ep.kind == 3) {
+        const T dn = ep.c2 * s;
+        ep.dnew[idx] = dn;
+        ep.x[idx] = dn;
       } else {
         const T dold = ep.dold[idx];
         const T dn = ep.c1 * dold + ep.c2 * s;
@@ -204,6 +207,15 @@ __device__ __forceinline__ void cheb_epilogue(const ChebEp<T>& ep, int64_t row, 
         ep.x[idx] += ep.add_old ? dn + dold : dn;
       }
     }
+}
+
+template <typename T, int BS, int L>
+__device__ __forceinline__ void cheb_epilogue(const ChebEp<T>& ep, int64_t row, const T* r) {
+  const T* D = ep.dinv + row * BS * BS;
+  T Dv[BS * BS];
+#pragma unroll
+  for (int q = 0; q < BS * BS; ++q) Dv[q] = D[q];
+  cheb_update<T, BS, L>(ep, row, r, Dv);
 }
 
 // --------------------------------------------------------------------------
@@ -567,63 +579,82 @@ k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint32_t* __restrict__
   }
 }
 
-// Chebyshev step as a separate pass (after an operator kernel that wrote r),
-// per node: the ChebEp update with dold and dnew allowed to coincide.
-template <typename T, int BS, int L>
-__global__ void k_cheb_step(int64_t n_nodes, ChebEp<T> ep, const T* __restrict__ r) {
-  TOPT_KERNEL_COUNT();
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_nodes;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    T rv[BS * L];
+// Inverted 3x3 diagonal block of node (ix, iy, iz) of the matrix-free
+// operator (block Jacobi): D = sum_c coef_c K0[la, la] over the <= 8 cells
+// around the node, fixed DOFs (bits of m) as identity rows / columns; FP32.
+// K0 comes from the constant bank (CONSTK) or from memory.
+template <bool CONSTK>
+__device__ __forceinline__ void mf_node_dinv(const MfGrid& g, const float* __restrict__ K0,
+                                             const float* __restrict__ coef, int m, int ix,
+                                             int iy, int iz, float* O) {
+  float D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
 #pragma unroll
-    for (int q = 0; q < BS * L; ++q) rv[q] = r[i * BS * L + q];
-    cheb_epilogue<T, BS, L>(ep, i, rv);
+  for (int la = 0; la < 8; ++la) {
+    const int cx = ix - hoff(la, 0), cy = iy - hoff(la, 1), cz = iz - hoff(la, 2);
+    if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
+    const float s = coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const int k = (3 * la + c) * 24 + 3 * la + d;
+        D[c * 3 + d] += s * (CONSTK ? c_K0f[k] : K0[k]);
+      }
   }
+  if (m) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+        if (((m >> c) & 1) || ((m >> d) & 1)) D[c * 3 + d] = (c == d) ? 1.0f : 0.0f;
+  }
+  const float A = D[4] * D[8] - D[5] * D[7], B = -(D[3] * D[8] - D[5] * D[6]),
+              C = D[3] * D[7] - D[4] * D[6];
+  const float det = D[0] * A + D[1] * B + D[2] * C;
+  const float si = det != 0.0f ? 1.0f / det : 0.0f;
+  O[0] = A * si;
+  O[1] = -(D[1] * D[8] - D[2] * D[7]) * si;
+  O[2] = (D[1] * D[5] - D[2] * D[4]) * si;
+  O[3] = B * si;
+  O[4] = (D[0] * D[8] - D[2] * D[6]) * si;
+  O[5] = -(D[0] * D[5] - D[2] * D[3]) * si;
+  O[6] = C * si;
+  O[7] = -(D[0] * D[7] - D[1] * D[6]) * si;
+  O[8] = (D[0] * D[4] - D[1] * D[3]) * si;
 }
 
-// Inverted 3x3 diagonal blocks of the matrix-free operator (block Jacobi, in
-// the operator's precision):
-// D_a = sum_c coef_c K0[la, la], fixed DOFs as identity rows / columns.
-template <typename T>
-__global__ void k_mf_diag_inv(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
-                              const uint8_t* __restrict__ mask, T* __restrict__ dinv) {
+// All blocks (stored for the power iteration and the generic smoother).
+__global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
+                              const float* __restrict__ coef, const uint8_t* __restrict__ mask,
+                              float* __restrict__ dinv) {
   TOPT_KERNEL_COUNT();
   const int ny1 = g.ny + 1, nx1 = g.nx + 1;
   const int64_t nn = (int64_t)nx1 * ny1 * (g.nz + 1);
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nn;
        a += (int64_t)gridDim.x * blockDim.x) {
     const int ai = (int)a;  // node counts fit 32 bits: cheap index math
-    const int iy = ai % ny1;
-    const int ix = (ai / ny1) % nx1;
-    const int iz = ai / (ny1 * nx1);
-    T D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    for (int la = 0; la < 8; ++la) {
-      const int cx = ix - c_hex_off[la][0], cy = iy - c_hex_off[la][1],
-                cz = iz - c_hex_off[la][2];
-      if (cx < 0 || cy < 0 || cz < 0 || cx >= g.nx || cy >= g.ny || cz >= g.nz) continue;
-      const T s = coef[cy + (int64_t)g.ny * (cx + (int64_t)g.nx * cz)];
-      for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d) D[c * 3 + d] += s * K0[(3 * la + c) * 24 + 3 * la + d];
-    }
-    if (mask) {
-      for (int c = 0; c < 3; ++c)
-        for (int d = 0; d < 3; ++d)
-          if (mask[a * 3 + c] || mask[a * 3 + d]) D[c * 3 + d] = (c == d) ? T(1) : T(0);
-    }
-    const T A = D[4] * D[8] - D[5] * D[7], B = -(D[3] * D[8] - D[5] * D[6]),
-            C = D[3] * D[7] - D[4] * D[6];
-    const T det = D[0] * A + D[1] * B + D[2] * C;
-    const T si = det != T(0) ? T(1) / det : T(0);
-    T* O = dinv + a * 9;
-    O[0] = A * si;
-    O[1] = -(D[1] * D[8] - D[2] * D[7]) * si;
-    O[2] = (D[1] * D[5] - D[2] * D[4]) * si;
-    O[3] = B * si;
-    O[4] = (D[0] * D[8] - D[2] * D[6]) * si;
-    O[5] = -(D[0] * D[5] - D[2] * D[3]) * si;
-    O[6] = C * si;
-    O[7] = -(D[0] * D[7] - D[1] * D[6]) * si;
-    O[8] = (D[0] * D[4] - D[1] * D[3]) * si;
+    const int iy = ai % ny1, ix = (ai / ny1) % nx1, iz = ai / (ny1 * nx1);
+    const int m = mask ? (mask[a * 3] | (mask[a * 3 + 1] << 1) | (mask[a * 3 + 2] << 2)) : 0;
+    mf_node_dinv<false>(g, K0, coef, m, ix, iy, iz, dinv + a * 9);
+  }
+}
+
+// Chebyshev step of the matrix-free fine level as a separate pass: the
+// inverted diagonal block is recomputed per node from the cell coefficients
+// (the same FP32 arithmetic as k_mf_diag_inv, so the same bits) instead of
+// being read, which saves 36 B per node.  m32: fixed-DOF bits per node.
+__global__ void k_cheb_mf(MfGrid g, const float* __restrict__ coef,
+                          const uint32_t* __restrict__ m32, ChebEp<float> ep,
+                          const float* __restrict__ r) {
+  TOPT_KERNEL_COUNT();
+  const int ny1 = g.ny + 1, nx1 = g.nx + 1;
+  const int nn = nx1 * ny1 * (g.nz + 1);
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nn; a += gridDim.x * blockDim.x) {
+    const int iy = a % ny1, ix = (a / ny1) % nx1, iz = a / (ny1 * nx1);
+    float rv[3] = {r[(int64_t)a * 3], r[(int64_t)a * 3 + 1], r[(int64_t)a * 3 + 2]};
+    float Dv[9];
+    mf_node_dinv<true>(g, nullptr, coef, (int)m32[a], ix, iy, iz, Dv);
+    cheb_update<float, 3, 1>(ep, a, rv, Dv);
   }
 }
 

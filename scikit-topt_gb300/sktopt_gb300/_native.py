@@ -53,7 +53,7 @@ class SolveOpts(C.Structure):
         ("method", C.c_int32), ("precond", C.c_int32), ("rtol", C.c_double),
         ("maxiter", C.c_int32), ("inner_rtol", C.c_double),
         ("max_outer", C.c_int32), ("cheb_degree", C.c_int32),
-        ("check_every", C.c_int32),
+        ("check_every", C.c_int32), ("cheb_ratio", C.c_double),
     ]
 
 

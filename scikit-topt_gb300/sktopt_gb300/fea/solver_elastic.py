@@ -54,6 +54,7 @@ class LinearSolverConfig:
     inner_rtol: float = 1e-1
     max_outer: int = 30
     cheb_degree: int = 2
+    cheb_ratio: float = 30.0       # smoother interval [lambda_max / ratio, lambda_max]
     check_every: int = 1
     direct_rtol: float = 1e-12
     mg_levels: int = 16
@@ -158,7 +159,8 @@ class FEM_SimpLinearElasticity:
         precond = 1 if eng.multigrid else 0
         comp, st = eng.solve(F, U, method, precond, cfg.resolved_rtol(),
                              cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
-                             cfg.cheb_degree, cfg.check_every)
+                             cfg.cheb_degree, cfg.check_every,
+                             cheb_ratio=cfg.cheb_ratio)
         self.last_stats = st
         self.solve_history.append(st)
         return comp

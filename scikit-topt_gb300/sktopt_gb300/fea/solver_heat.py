@@ -82,7 +82,8 @@ class FEM_SimpLinearHeatConduction:
             {"fcg": 3, "replace": 4, "reliable": 1, "restart": 2}[cfg.refine]
         _, st = eng.solve(self._F, U, method, 1 if eng.multigrid else 0, cfg.resolved_rtol(),
                           cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
-                          cfg.cheb_degree, cfg.check_every)
+                          cfg.cheb_degree, cfg.check_every,
+                             cheb_ratio=cfg.cheb_ratio)
         self.last_stats = st
         self.solve_history.append(st)
         KT = eng.spmv(U)
