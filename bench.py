@@ -134,13 +134,35 @@ def make_optimizer(size, precision, max_iters, device):
     return opt
 
 
+def replica_barrier():
+    """Barrier across the replicas (no-op for one process)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.barrier()
+
+
+def replica_max(t):
+    """Maximum of a per-replica time over all replicas (the job's time)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1):
+        return float(t)
+    dev = torch.device("cuda", torch.cuda.current_device()) \
+        if dist.get_backend() == "nccl" else torch.device("cpu")
+    tt = torch.tensor([float(t)], dtype=torch.float64, device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def timed_run(opt, warmup, steps, sampler=None, label="steps"):
     """Warm-up, then `steps` OC iterations timed with CUDA events (NVTX range
-    `label`, for profiler filtering)."""
+    `label`, for profiler filtering), bracketed by a replica barrier and a
+    device synchronisation on both sides."""
     import torch
     for _ in range(warmup):
         opt.optimize_steps(1)
     torch.cuda.synchronize()
+    replica_barrier()
     from sktopt_gb300 import _native
     l0 = _native.launch_count()
     s = torch.cuda.current_stream()
@@ -156,6 +178,7 @@ def timed_run(opt, warmup, steps, sampler=None, label="steps"):
     e1.record(s)
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
+    replica_barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop() if sampler else None
     l1 = _native.launch_count()
@@ -287,12 +310,7 @@ def run_gpu(args):
                 "solver_iters": [(s.iters, s.relres) for s in o64.fem.solve_history][-args.steps:]}
         del o64
     # max over ranks
-    t_step = ms * 1e-3
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_step], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step = float(tt.item())
+    t_step = replica_max(ms * 1e-3)
     value = args.steps / t_step * world
     if args.phases and rank == 0:
         print(json.dumps({"phases_ms_mixed": phases}), file=sys.stderr)
