@@ -127,6 +127,9 @@ typedef struct topt_solve_opts {
   int32_t cheb_degree;    /* Chebyshev smoother degree                       */
   int32_t check_every;    /* residual check period (iterations)              */
   double cheb_ratio;      /* Chebyshev interval [lmax/ratio, lmax] (0: 30)   */
+  int32_t x0;             /* methods 0, 3, 4: start from U (its fixed DOFs are
+                             zeroed) instead of 0; same stopping rule          */
+  int32_t pad;
 } topt_solve_opts;
 
 typedef struct topt_solve_info {

@@ -103,6 +103,7 @@ struct topt_fem {
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   int interp = 0;                      // 0 SIMP, 1 RAMP
   double cheb_ratio = 30.0;            // smoother interval [lmax/ratio, lmax]
+  bool x0 = false;                     // this solve starts from the caller's U
   bool assembled = false;
   // matrix-free FP32 level-0 operator (uniform hex grid, shared unit matrix)
   bool mf = false;
@@ -957,6 +958,18 @@ static int precond_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int p
   return TOPT_OK;
 }
 
+// Zero the fixed DOFs of an initial guess (FP64 solution vectors; the FP32
+// hierarchy is never started from a guess).
+template <typename T>
+static int start_from(topt_fem* h, int L, T* x) {
+  if (std::is_same<T, double>::value) {
+    k_zero_fixed<<<gridsize(h, h->n_dof * L), kBlock, 0, h->stream>>>(
+        h->n_dof, L, h->mask.as<uint8_t>(), (double*)x);
+    TOPT_CHECK_LAUNCH("k_zero_fixed");
+  }
+  return TOPT_OK;
+}
+
 // Mixed precision PCG with reliable updates: CG recurrences, operator and
 // preconditioner in FP32; whenever the FP32 residual has dropped by `delta`
 // since the last update (or looks converged) the FP32 iterate is added to the
@@ -1056,7 +1069,7 @@ static int pcg_reliable(topt_fem* h, int L, double* U, float* p32, float* q32, f
 template <typename T>
 static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* z, T* r,
                double rtol, int maxiter, int precond, int degree, int check_every,
-               int* iters_out, double* relres_out, int* status) {
+               int* iters_out, double* relres_out, int* status, bool x0 = false) {
   LevelStruct& L0 = h->ls[0];
   LevelNum<T>& N0 = H.lv[0];
   const int bs = h->bs;
@@ -1067,8 +1080,13 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   double bnorm2[4] = {0, 0, 0, 0};
   if ((rc = dot<T>(h, n, L, b, b, 2))) return rc;
   if ((rc = read_slot(h, 2, L, bnorm2))) return rc;
-  TOPT_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * nl, h->stream));
-  TOPT_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * nl, cudaMemcpyDeviceToDevice, h->stream));
+  if (x0) {   // r = b - A x from the caller's x (fixed DOFs zeroed first)
+    if ((rc = start_from(h, L, x))) return rc;
+    if ((rc = spmv<T>(h, L0, bs, L, 1, false, vals, x, b, r))) return rc;
+  } else {
+    TOPT_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * nl, h->stream));
+    TOPT_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * nl, cudaMemcpyDeviceToDevice, h->stream));
+  }
   // device scalars: slots 3 (rz A), 4 (rz B), 5 (pq), 6 (rr); active flags
   int active_h[4] = {1, 1, 1, 1};
   for (int j = 0; j < L; ++j)
@@ -1147,9 +1165,15 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   DevBuf& active = h->active;
   TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
                             h->stream));
-  TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
-  TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice, h->stream));
-  k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
+  if (h->x0) {   // r = Fe - K U from the caller's U (fixed DOFs zeroed first)
+    if ((rc = start_from<double>(h, L, U))) return rc;
+    if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r))) return rc;
+  } else {
+    TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
+    TOPT_CUDA(cudaMemcpyAsync(r, fe, sizeof(double) * nl, cudaMemcpyDeviceToDevice,
+                              h->stream));
+  }
+  k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r, r32);
   TOPT_CHECK_LAUNCH("k_convert");
   // z = M32(r); slot 3 <- r.z (FP64 r, FP32 z)
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
@@ -1238,8 +1262,16 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* r64, float* p32, fl
   DevBuf& active = h->active;
   TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
                             h->stream));
-  TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
-  k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
+  if (h->x0) {   // r = Fe - K U from the caller's U (fixed DOFs zeroed first)
+    if ((rc = start_from<double>(h, L, U))) return rc;
+    if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r64))) return rc;
+    if ((rc = dot<double>(h, n, L, r64, r64, 7))) return rc;
+    if ((rc = read_slot(h, 7, L, rlast2))) return rc;
+    k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, r64, r32);
+  } else {
+    TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
+    k_convert<float, double><<<gridsize(h, nl), kBlock, 0, h->stream>>>(nl, fe, r32);
+  }
   TOPT_CHECK_LAUNCH("k_convert");
   if ((rc = precond_apply<float>(h, H, L, r32, z32, precond, degree, -1))) return rc;
   TOPT_L_DISPATCH(L, (k_dot2<float, float, float, L_><<<gridsize(h, n), kBlock, 0, h->stream>>>(
@@ -1555,6 +1587,7 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
   const int check = o->check_every > 0 ? o->check_every : 1;
   const int degree = o->cheb_degree > 0 ? o->cheb_degree : 2;
   h->cheb_ratio = o->cheb_ratio > 1.0 ? o->cheb_ratio : 30.0;
+  h->x0 = o->x0 != 0 && (o->method == 0 || o->method == 3 || o->method == 4);
   int rc;
   topt_solve_info inf{};
   k_enforce_rhs<<<gridsize(h, nl), kBlock, 0, h->stream>>>(n, L, h->mask.as<uint8_t>(), F,
@@ -1566,7 +1599,8 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
   double* r = z + nl;
   if (o->method == 0) {
     if ((rc = pcg<double>(h, h->h64, L, h->fe.as<double>(), U, p, q, z, r, o->rtol, o->maxiter,
-                          o->precond, degree, check, &inf.iters, &inf.relres, &inf.status)))
+                          o->precond, degree, check, &inf.iters, &inf.relres, &inf.status,
+                          h->x0)))
       return rc;
   } else if (o->method == 3) {
     // FP64 flexible CG, FP32 multigrid inner solve; U0 holds p, q, r (FP64)

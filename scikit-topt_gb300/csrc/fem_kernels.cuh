@@ -1095,6 +1095,14 @@ __global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
        i += (int64_t)gridDim.x * blockDim.x)
     u[i] += (double)d[i];
 }
+// U[fixed DOFs] = 0 (an initial guess of the enforced system).
+__global__ void k_zero_fixed(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
+                             double* __restrict__ u) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof * L;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if (mask[i / L]) u[i] = 0.0;
+}
 // F_e: copy of F with fixed DOFs zeroed (enforce's RHS with x = 0).
 __global__ void k_enforce_rhs(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
                               const double* __restrict__ f, double* __restrict__ fe) {

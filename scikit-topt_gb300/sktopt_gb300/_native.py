@@ -54,6 +54,7 @@ class SolveOpts(C.Structure):
         ("maxiter", C.c_int32), ("inner_rtol", C.c_double),
         ("max_outer", C.c_int32), ("cheb_degree", C.c_int32),
         ("check_every", C.c_int32), ("cheb_ratio", C.c_double),
+        ("x0", C.c_int32), ("pad", C.c_int32),
     ]
 
 

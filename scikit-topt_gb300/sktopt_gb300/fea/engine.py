@@ -105,14 +105,15 @@ class FemEngine:
     def solve(self, F: torch.Tensor, U: torch.Tensor, method: int, precond: int, rtol: float,
               maxiter: int, inner_rtol: float = 1e-4, max_outer: int = 20,
               cheb_degree: int = 2, check_every: int = 1, raise_on_maxiter=False,
-              cheb_ratio: float = 30.0):
-        """Solve K_e U = F_e for every column; returns (compliance, SolveStats)."""
+              cheb_ratio: float = 30.0, x0: bool = False):
+        """Solve K_e U = F_e for every column; returns (compliance, SolveStats).
+        With x0 the solve starts from the U passed in (fixed DOFs zeroed)."""
         self._bind()
         L = F.shape[1] if F.dim() == 2 else 1
         o = N.SolveOpts(method=method, precond=precond, rtol=rtol, maxiter=maxiter,
                         inner_rtol=inner_rtol, max_outer=max_outer,
                         cheb_degree=cheb_degree, check_every=check_every,
-                        cheb_ratio=cheb_ratio)
+                        cheb_ratio=cheb_ratio, x0=1 if x0 else 0)
         info = N.SolveInfo()
         comp = np.zeros(L)
         N.check(self.lib.topt_fem_solve(self.h, C.c_void_p(F.data_ptr()),

@@ -17,6 +17,10 @@ fields (solver_elastic.py:34-40) and adds the GPU choices:
   and replaces the FP32 residual by the FP64 one whenever it has dropped by
   ``inner_rtol``; "restart" restarts an FP32 PCG to ``inner_rtol`` for every
   FP64 refinement step.
+* ``warm_start``: each solve starts from the ``U`` it is given (the previous
+  solution in the optimisation loop) instead of zero; convergence is still
+  ``||Fe - K U|| <= rtol ||Fe||``, so the accepted solutions meet the
+  reference's tolerance (the reference's SciPy CG starts from zero).
 * ``precond``: "mg" (multigrid V-cycle on the logical grid) or "jacobi"
   (3x3 block Jacobi; what the reference's ``cg_jacobi`` uses as scalar Jacobi).
 
@@ -55,6 +59,9 @@ class LinearSolverConfig:
     max_outer: int = 30
     cheb_degree: int = 2
     cheb_ratio: float = 30.0       # smoother interval [lambda_max / ratio, lambda_max]
+    # start each solve from the U passed in (the previous design's solution in
+    # the optimisation loop) instead of 0; the stopping rule is unchanged
+    warm_start: bool = True
     check_every: int = 1
     direct_rtol: float = 1e-12
     mg_levels: int = 16
@@ -160,7 +167,7 @@ class FEM_SimpLinearElasticity:
         comp, st = eng.solve(F, U, method, precond, cfg.resolved_rtol(),
                              cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
                              cfg.cheb_degree, cfg.check_every,
-                             cheb_ratio=cfg.cheb_ratio)
+                             cheb_ratio=cfg.cheb_ratio, x0=cfg.warm_start)
         self.last_stats = st
         self.solve_history.append(st)
         return comp
@@ -175,7 +182,7 @@ class FEM_SimpLinearElasticity:
                 and u_dofs.dtype == torch.float64:
             U = u_dofs.view(-1, L)
         else:
-            U = torch.empty((self.engine.n_dof, L), dtype=torch.float64, device=self.device)
+            U = as_device(u_dofs, device=self.device).reshape(self.engine.n_dof, L).clone()
         comp = self.solve_device(rho_d, p, U, force_scale)
         write_back(u_dofs, U)
         return comp

@@ -83,7 +83,7 @@ class FEM_SimpLinearHeatConduction:
         _, st = eng.solve(self._F, U, method, 1 if eng.multigrid else 0, cfg.resolved_rtol(),
                           cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
                           cfg.cheb_degree, cfg.check_every,
-                             cheb_ratio=cfg.cheb_ratio)
+                          cheb_ratio=cfg.cheb_ratio, x0=cfg.warm_start)
         self.last_stats = st
         self.solve_history.append(st)
         KT = eng.spmv(U)
@@ -106,7 +106,7 @@ class FEM_SimpLinearHeatConduction:
                 and u_dofs.dtype == torch.float64:
             U = u_dofs.view(-1, 1)
         else:
-            U = torch.empty((self.engine.n_dof, 1), dtype=torch.float64, device=self.device)
+            U = as_device(u_dofs, device=self.device).reshape(self.engine.n_dof, 1).clone()
         J = self.solve_device(rho_d, p, U)
         write_back(u_dofs, U)
         return J
