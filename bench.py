@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
-    ap.add_argument("--probe", choices=["spmv", "solve", "batch"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd"], default=None,
                     help="profiling target instead of the benchmark")
     return ap.parse_args()
 
@@ -533,6 +533,60 @@ def probe_batch(n_designs, iters, workers):
     print(json.dumps(out))
 
 
+def probe_autograd(size=(100, 50, 50)):
+    """Differentiation workload: compliance(rho) and thermal compliance(rho)
+    as autograd Functions on a 100x50x50 hex grid, rho ~ U(0.1, 1) (seed 0),
+    p = 3; elasticity with the cantilever supports, heat with k0 = 1,
+    kmin = 1e-3, unit source and T = 0 on a centred 10x10 patch of z = 0.
+    Times forward + backward (FP64 and mixed solves) and checks the gradient
+    against central differences (step 1e-6) along two random directions."""
+    import numpy as np
+    import torch
+    from sktopt_gb300.core.autograd import compliance
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.fea.solver_heat import FEM_SimpLinearHeatConduction
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", 0)
+    out = {"probe": "autograd", "size": list(size)}
+    for phys in ("elasticity", "heat"):
+        tsk = toy_problem.cantilever(*size) if phys == "elasticity" else \
+            toy_problem.heat_box(*size, patch=10)
+        g = np.random.default_rng(0)
+        rho = torch.from_numpy(0.1 + 0.9 * g.random(tsk.mesh.nelements)).to(dev)
+        for prec in ("fp64", "mixed"):
+            cfg = LinearSolverConfig(solver="cg_pyamg", rtol=1e-10, precision=prec)
+            fem = FEM_SimpLinearElasticity(tsk, 1e-9, solver_config=cfg, device=dev) \
+                if phys == "elasticity" else \
+                FEM_SimpLinearHeatConduction(tsk, 1e-3, solver_config=cfg, device=dev)
+            x = rho.clone().requires_grad_(True)
+            compliance(x, fem, 3.0).backward()          # warm-up (engine, hierarchy)
+            x = rho.clone().requires_grad_(True)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            C = compliance(x, fem, 3.0)
+            C.backward()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            rec = {"forward_backward_ms": round(dt * 1e3, 1), "compliance": float(C.detach())}
+            if prec == "fp64":
+                h = 1e-6
+                errs = []
+                for k in range(2):
+                    d = torch.from_numpy(np.random.default_rng(10 + k).standard_normal(
+                        rho.numel())).to(dev)
+                    with torch.no_grad():
+                        cp = float(compliance(rho + h * d, fem, 3.0))
+                        cm = float(compliance(rho - h * d, fem, 3.0))
+                    fd = (cp - cm) / (2 * h)
+                    ad = float(torch.dot(x.grad, d))
+                    errs.append(abs(fd - ad) / abs(fd))
+                rec["grad_vs_central_difference_rel"] = [float(f"{e:.2e}") for e in errs]
+            out[f"{phys}_{prec}"] = rec
+            del fem
+            torch.cuda.empty_cache()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.probe == "spmv":
@@ -543,6 +597,9 @@ def main():
         return
     if args.probe == "batch":
         probe_batch(32, 6, 16)
+        return
+    if args.probe == "autograd":
+        probe_autograd()
         return
     if args.impl == "reference":
         run_reference(args)
