@@ -35,6 +35,7 @@ extern "C" {
 /* value types */
 #define TOPT_F64 0
 #define TOPT_F32 1
+#define TOPT_F64_FULL 2   /* topt_fem_spmv: FP64 operator before enforcement */
 
 const char* topt_version(void);
 const char* topt_last_error(void);
@@ -105,8 +106,20 @@ int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin,
 /* Material interpolation of the later topt_fem_update / topt_fem_energy calls:
  * kind 0 SIMP (default; composer.py:19-22, dC_drho_simp derivatives.py:25-52),
  * 1 RAMP E = Emin + (E0 - Emin) rho / (1 + p (1 - rho)) (composer.py:25-39,
- * dC_drho_ramp derivatives.py:56-72), p being the RAMP parameter. */
+ * dC_drho_ramp derivatives.py:56-72), p being the RAMP parameter; 2 the RAMP
+ * operator and energy with the dC_drho_simp sensitivity (the heat plugin's
+ * compliance_sensitivity_multi_load, solver_heat.py:928-950). */
 int topt_fem_set_interpolation(topt_fem* h, int32_t kind);
+
+/* Per-element matrices added, unscaled, to coef_e Ke in the level-0 operator,
+ * its Galerkin coarse levels and the TOPT_F64_FULL product from the next
+ * topt_fem_update on (the Robin terms of solve_multi_load,
+ * solver_heat.py:198-253).  extra: dev, n_elem x (bs nloc)^2 FP64, row-major
+ * per element, kept by pointer (the caller keeps it alive and refreshes it
+ * before each update); NULL removes the terms.  Element energies and
+ * sensitivities (topt_fem_energy) keep the conduction part only.  Not
+ * available on handles with the matrix-free FP32 operator. */
+int topt_fem_set_element_extra(topt_fem* h, const double* extra);
 
 typedef struct topt_solve_opts {
   int32_t method;         /* 0: FP64 PCG.  Mixed (FP32 operator, hierarchy and
@@ -150,7 +163,10 @@ int topt_fem_solve(topt_fem* h, const double* F, double* U, int32_t nrhs,
                    double* compliance);
 
 /* y = K x with the enforced operator (dtype TOPT_F64 or TOPT_F32; F32 needs
- * mixed).  x, y: dev, n_dof x nrhs row-major. */
+ * mixed), or with the FP64 operator before enforcement (TOPT_F64_FULL: the
+ * K_csr of solve_multi_load, solver_heat.py:220-237, used for T^T K T and for
+ * nonzero Dirichlet values; assembled on first use after each update).
+ * x, y: dev, n_dof x nrhs row-major. */
 int topt_fem_spmv(topt_fem* h, int32_t dtype, const void* x, void* y,
                   int32_t nrhs);
 
@@ -280,6 +296,52 @@ int topt_elem_to_node(int64_t n_nodes, const int32_t* node_ptr, const int32_t* n
                       double fixed_value, double* out, void* stream);
 int topt_node_to_elem(int64_t n_elem, int32_t nloc, const int32_t* t, const double* x_node,
                       int32_t clamp_nonpositive, double* out, void* stream);
+
+/* ------------------------------------------------------------------------
+ * Heat plugin on hexahedral meshes (FEM_SimpLinearHeatConduction,
+ * sktopt/fea/solver_heat.py:306-625, 705-980): Robin terms, heat-exchange
+ * objective and adjoint load, explicit Robin gradient, grad T . grad lam.
+ * Cells must be axis-aligned boxes; volume integrals use the 2x2x2 Gauss
+ * rule.  Vectors are dev, n_nodes (x L row-major for several columns).
+ * ---------------------------------------------------------------------- */
+typedef struct topt_heat topt_heat;
+/* t: host, 8 x n_elem (row a = local node a, MeshHex order); p: host,
+ * 3 x n_nodes.  pairing 0 gives the nodal density average the reference's
+ * pairing of t.ravel() with np.repeat(rho, 8) (solver_heat.py:600-613,
+ * 730-737: node t[a][e] receives rho[(a n_elem + e) / 8]); 1 gives node
+ * t[a][e] the density of element e. */
+int topt_heat_create(int64_t n_nodes, int64_t n_elem, const int32_t* t, const double* p,
+                     int32_t pairing, topt_heat** out);
+void topt_heat_destroy(topt_heat* h);
+int topt_heat_set_stream(topt_heat* h, void* cuda_stream);
+/* Surface Robin matrices h int N_a N_b over the Robin facets
+ * (assemble_surface_robin task_heat.py:60-139), one 8 x 8 per facet in the
+ * owning element's local numbering.  elems, mats: host. */
+int topt_heat_set_surface(topt_heat* h, int64_t n_faces, const int32_t* elems,
+                          const double* mats);
+/* rho_node = the nodal average of the element densities rho. */
+int topt_heat_nodal_average(topt_heat* h, const double* rho, double* rho_node);
+/* extra (dev, n_elem x 64) = virtual Robin element matrices
+ * (get_robin_virtual solver_heat.py:552-572; when virtual_on) + surface
+ * matrices; load (dev, may be NULL) = the virtual Robin load. */
+int topt_heat_robin(topt_heat* h, const double* rho_node, double h_coef, double t_env,
+                    double p, double q, int32_t virtual_on, double* extra, double* load);
+/* den = int |grad rho| and num[j] = int -T_env h (T_j - T_env) |grad rho|
+ * (solver_heat.py:306-321, 382-390, 411-440) for L <= 4 columns of T
+ * (L = 0: den only).  den, num: host. */
+int topt_heat_exchange(topt_heat* h, const double* rho_node, const double* T, int32_t L,
+                       double h_coef, double t_env, double* den, double* num);
+/* rhs = (int -T_env h_eff |grad rho| v) / den, h_eff the interpolated nodal
+ * h rho^p (1 - rho)^q (solver_heat.py:392-408, 825-832); den > 0. */
+int topt_heat_exchange_adjoint(topt_heat* h, const double* rho_node, double h_coef,
+                               double t_env, double p, double q, double den, double* rhs);
+/* grad (dev, n_elem x L) += the explicit Robin gradient of the compliance
+ * objective (solver_heat.py:575-597 mapped by 616-625, 952-979). */
+int topt_heat_robin_grad(topt_heat* h, const double* rho_node, const double* T, int32_t L,
+                         double h_coef, double t_env, double p, double q, double* grad);
+/* out (dev, n_elem x L) = int_e grad X_j . grad Y_j (solver_heat.py:324-379,
+ * 529-550). */
+int topt_heat_grad_dot(topt_heat* h, const double* X, const double* Y, int32_t L, double* out);
 
 /* Dot product that allocates no device memory, for callers that cannot call
  * cudaMalloc (a host whose device memory is owned by its own pool, or a loop

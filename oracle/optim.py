@@ -175,8 +175,16 @@ class OracleOptimizer:
         energy = self.pb.energy(rho_p, p, Emin, U)
         dH = heaviside_projection_derivative(rho_f, beta, cfg.beta_eta)
         dC_full = np.zeros_like(self.rho)
+        # FEM plugins with compliance_sensitivity_multi_load supply their own
+        # sensitivity (common_density.py:1068-1085)
+        custom = self.pb.custom_sensitivity(rho_p, p, Emin, U) \
+            if hasattr(self.pb, "custom_sensitivity") else None
         for i in range(U.shape[1]):
-            dCp = fem.sensitivity(cfg.interpolation)(rho_p, energy[:, i], self.pb.E0, Emin, p)
+            if custom is not None:
+                dCp = custom[:, i]
+            else:
+                dCp = fem.sensitivity(cfg.interpolation)(rho_p, energy[:, i], self.pb.E0,
+                                                         Emin, p)
             dC_full += self.filt.gradient(dCp * dH)
         dC_full /= U.shape[1]
         dC_d = dC_full[self.design].copy()

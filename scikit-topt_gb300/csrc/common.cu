@@ -45,6 +45,9 @@ extern "C" int topt_launch_count(uint64_t* out) {
   unsigned long long c = 0;
   rc = topt::launches_design(&c);
   if (rc) return rc;
-  *out = (uint64_t)(a + b + c);
+  unsigned long long d = 0;
+  rc = topt::launches_heat(&d);
+  if (rc) return rc;
+  *out = (uint64_t)(a + b + c + d);
   return TOPT_OK;
 }

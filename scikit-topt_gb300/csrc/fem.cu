@@ -101,7 +101,13 @@ struct topt_fem {
   topt::DevBuf active;                 // per-load "still iterating" flags (4 ints)
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
-  int interp = 0;                      // 0 SIMP, 1 RAMP
+  int interp = 0;                      // 0 SIMP, 1 RAMP, 2 RAMP / SIMP-form sensitivity
+  // per-element matrices added to coef_e Ke at level 0 (caller's device
+  // buffer, n_elem x (bs nloc)^2 FP64; the heat plugin's Robin terms)
+  const double* extra64 = nullptr;
+  topt::DevBuf extra32;                // FP32 copy for the mixed hierarchy
+  topt::DevBuf full64;                 // level-0 FP64 operator without enforcement
+  bool full_ok = false;                // full64 holds the current operator
   double cheb_ratio = 30.0;            // smoother interval [lmax/ratio, lmax]
   bool x0 = false;                     // this solve starts from the caller's U
   bool assembled = false;
@@ -292,22 +298,27 @@ static int make_transfer(LevelStruct& F, const LevelStruct& Cs, cudaStream_t s) 
 // ---------------------------------------------------------------- dispatch helpers
 template <typename T, int BS, int NLOC>
 static int launch_assemble(topt_fem* h, const LevelStruct& L, const T* ke, int64_t ke_stride,
-                           const T* coef, const uint8_t* mask, T* vals) {
+                           const T* coef, const T* extra, const uint8_t* mask, T* vals) {
   const size_t sh = ke_stride == 0 ? sizeof(T) * BS * NLOC * BS * NLOC : 0;
   k_assemble<T, BS, NLOC><<<gridsize(h, L.npos), kBlock, sh, h->stream>>>(
-      L.npos, L.sell, L.cptr.as<int64_t>(), L.contrib.as<int32_t>(), ke, ke_stride, coef, mask,
-      vals);
+      L.npos, L.sell, L.cptr.as<int64_t>(), L.contrib.as<int32_t>(), ke, ke_stride, coef, extra,
+      mask, vals);
   TOPT_CHECK_LAUNCH("k_assemble");
   return TOPT_OK;
 }
 
 template <typename T>
 static int assemble(topt_fem* h, const LevelStruct& L, int bs, int nloc, const T* ke,
-                    int64_t ke_stride, const T* coef, const uint8_t* mask, T* vals) {
-  if (bs == 3 && nloc == 8) return launch_assemble<T, 3, 8>(h, L, ke, ke_stride, coef, mask, vals);
-  if (bs == 3 && nloc == 4) return launch_assemble<T, 3, 4>(h, L, ke, ke_stride, coef, mask, vals);
-  if (bs == 1 && nloc == 8) return launch_assemble<T, 1, 8>(h, L, ke, ke_stride, coef, mask, vals);
-  if (bs == 1 && nloc == 4) return launch_assemble<T, 1, 4>(h, L, ke, ke_stride, coef, mask, vals);
+                    int64_t ke_stride, const T* coef, const T* extra, const uint8_t* mask,
+                    T* vals) {
+  if (bs == 3 && nloc == 8)
+    return launch_assemble<T, 3, 8>(h, L, ke, ke_stride, coef, extra, mask, vals);
+  if (bs == 3 && nloc == 4)
+    return launch_assemble<T, 3, 4>(h, L, ke, ke_stride, coef, extra, mask, vals);
+  if (bs == 1 && nloc == 8)
+    return launch_assemble<T, 1, 8>(h, L, ke, ke_stride, coef, extra, mask, vals);
+  if (bs == 1 && nloc == 4)
+    return launch_assemble<T, 1, 4>(h, L, ke, ke_stride, coef, extra, mask, vals);
   return fail(TOPT_BAD_INPUT, "assemble: unsupported bs/nloc");
 }
 
@@ -499,6 +510,11 @@ template <typename T>
 static const T* level0_coef(topt_fem* h) {
   return std::is_same<T, double>::value ? (const T*)h->coef64.p : (const T*)h->coef32.p;
 }
+template <typename T>
+static const T* level0_extra(topt_fem* h) {
+  if (!h->extra64) return nullptr;
+  return std::is_same<T, double>::value ? (const T*)h->extra64 : (const T*)h->extra32.p;
+}
 
 template <typename T>
 static int alloc_level_num(topt_fem* h, LevelNum<T>& N, const LevelStruct& L, int li) {
@@ -527,6 +543,7 @@ static int galerkin(topt_fem* h, int li, Hier<T>& H) {
   const int64_t stride = lvl0 ? (h->n_ke == 1 ? 0 : (int64_t)(bs * h->nloc) * (bs * h->nloc))
                               : (int64_t)(bs * 8) * (bs * 8);
   const T* coef = lvl0 ? level0_coef<T>(h) : nullptr;
+  const T* extra = lvl0 ? level0_extra<T>(h) : nullptr;
   const uint8_t* mask = lvl0 ? h->mask.as<uint8_t>() : nullptr;
   const int32_t* cptr = (lvl0 && F.cell_ptr.p) ? F.cell_ptr.as<int32_t>() : nullptr;
   const int32_t* cel = (lvl0 && F.cell_ptr.p) ? F.cell_elems.as<int32_t>() : nullptr;
@@ -534,7 +551,7 @@ static int galerkin(topt_fem* h, int li, Hier<T>& H) {
   int64_t ncells = (int64_t)F.grid.ncx * F.grid.ncy * F.grid.ncz;
   T* out = H.lv[li + 1].ke.template as<T>();
   const int32_t* list = nullptr;
-  if (lvl0 && F.gal_shared) {
+  if (lvl0 && F.gal_shared && !extra) {
     const T* M = std::is_same<T, double>::value ? (const T*)F.gal_M64.p : (const T*)F.gal_M32.p;
     const int g = (int)std::min<int64_t>(ncells, (int64_t)h->sm * 32);
     if (bs == 3)
@@ -551,19 +568,19 @@ static int galerkin(topt_fem* h, int li, Hier<T>& H) {
   if (bs == 3 && nloc == 8)
     k_galerkin<T, 3, 8><<<ncells, 256, 0, h->stream>>>(F.grid, list, cptr, cel,
                                                        F.t.as<int32_t>(), F.n_elem, ke, stride,
-                                                       coef, mask, out);
+                                                       coef, extra, mask, out);
   else if (bs == 3 && nloc == 4)
     k_galerkin<T, 3, 4><<<ncells, 256, 0, h->stream>>>(F.grid, list, cptr, cel,
                                                        F.t.as<int32_t>(), F.n_elem, ke, stride,
-                                                       coef, mask, out);
+                                                       coef, extra, mask, out);
   else if (bs == 1 && nloc == 8)
     k_galerkin<T, 1, 8><<<ncells, 256, 0, h->stream>>>(F.grid, list, cptr, cel,
                                                        F.t.as<int32_t>(), F.n_elem, ke, stride,
-                                                       coef, mask, out);
+                                                       coef, extra, mask, out);
   else
     k_galerkin<T, 1, 4><<<ncells, 256, 0, h->stream>>>(F.grid, list, cptr, cel,
                                                        F.t.as<int32_t>(), F.n_elem, ke, stride,
-                                                       coef, mask, out);
+                                                       coef, extra, mask, out);
   TOPT_CHECK_LAUNCH("k_galerkin");
   return TOPT_OK;
 }
@@ -760,7 +777,7 @@ static int refresh(topt_fem* h, Hier<T>& H) {
     TOPT_CHECK_LAUNCH("k_mf_diag_inv");
   } else {
     if ((rc = assemble<T>(h, h->ls[0], bs, h->nloc, level0_ke<T>(h), stride0,
-                          level0_coef<T>(h), h->mask.as<uint8_t>(),
+                          level0_coef<T>(h), level0_extra<T>(h), h->mask.as<uint8_t>(),
                           H.lv[0].vals.template as<T>())))
       return rc;
     if ((rc = block_inv<T>(h, h->ls[0], H.lv[0].vals.template as<T>(),
@@ -774,7 +791,7 @@ static int refresh(topt_fem* h, Hier<T>& H) {
     if (li > 0) {
       if ((rc = galerkin<T>(h, li - 1, H))) return rc;
       if ((rc = assemble<T>(h, L, bs, 8, N.ke.template as<T>(), (int64_t)(bs * 8) * (bs * 8),
-                            nullptr, nullptr, N.vals.template as<T>())))
+                            nullptr, nullptr, nullptr, N.vals.template as<T>())))
         return rc;
       if ((rc = block_inv<T>(h, L, N.vals.template as<T>(), N.dinv.template as<T>(), true)))
         return rc;
@@ -1504,8 +1521,8 @@ int topt_fem_sizes(const topt_fem* h, int64_t* n_dof, int64_t* nnzb, int32_t* n_
 
 int topt_fem_set_interpolation(topt_fem* h, int32_t kind) {
   if (!h) return fail(TOPT_BAD_INPUT, "fem_set_interpolation: null handle");
-  if (kind != 0 && kind != 1)
-    return fail(TOPT_BAD_INPUT, "fem_set_interpolation: kind must be 0 (SIMP) or 1 (RAMP)");
+  if (kind < 0 || kind > 2)
+    return fail(TOPT_BAD_INPUT, "fem_set_interpolation: kind must be 0 (SIMP), 1 (RAMP) or 2 (RAMP, SIMP-form sensitivity)");
   h->interp = kind;
   return TOPT_OK;
 }
@@ -1518,6 +1535,15 @@ int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin, doub
       h->mixed ? h->coef32.as<float>() : nullptr, h->interp);
   TOPT_CHECK_LAUNCH("k_simp_coef");
   int rc;
+  h->full_ok = false;
+  if (h->extra64 && h->mixed) {
+    const int64_t nx = h->n_elem * (int64_t)(h->bs * h->nloc) * (h->bs * h->nloc);
+    if (h->extra32.bytes < sizeof(float) * (size_t)nx &&
+        (rc = h->extra32.alloc(sizeof(float) * (size_t)nx)))
+      return rc;
+    k_d2f<<<gridsize(h, nx), kBlock, 0, h->stream>>>(nx, h->extra64, h->extra32.as<float>());
+    TOPT_CHECK_LAUNCH("k_d2f");
+  }
   if (h->mixed) {
     // FP64 operator for the refinement residual, FP32 operator + hierarchy
     if (!h->vals64_0.p &&
@@ -1525,7 +1551,7 @@ int topt_fem_update(topt_fem* h, const double* rho, double E0, double Emin, doub
       return rc;
     const int64_t stride0 = h->n_ke == 1 ? 0 : (int64_t)(h->bs * h->nloc) * (h->bs * h->nloc);
     if ((rc = assemble<double>(h, h->ls[0], h->bs, h->nloc, h->ke64.as<double>(), stride0,
-                               h->coef64.as<double>(), h->mask.as<uint8_t>(),
+                               h->coef64.as<double>(), h->extra64, h->mask.as<uint8_t>(),
                                h->vals64_0.as<double>())))
       return rc;
     if ((rc = refresh<float>(h, h->h32))) return rc;
@@ -1541,10 +1567,36 @@ static const double* op64(topt_fem* h) {
   return h->mixed ? h->vals64_0.as<double>() : h->h64.lv[0].vals.as<double>();
 }
 
+int topt_fem_set_element_extra(topt_fem* h, const double* extra) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_element_extra: null handle");
+  if (extra && h->mf)
+    return fail(TOPT_BAD_INPUT,
+                "fem_set_element_extra: the matrix-free level-0 operator takes no extra terms");
+  h->extra64 = extra;
+  h->assembled = false;
+  return TOPT_OK;
+}
+
 int topt_fem_spmv(topt_fem* h, int32_t dtype, const void* x, void* y, int32_t nrhs) {
   if (!h || !x || !y) return fail(TOPT_BAD_INPUT, "fem_spmv: null argument");
   if (!h->assembled) return fail(TOPT_BAD_INPUT, "fem_spmv: call topt_fem_update first");
   if (nrhs < 1 || nrhs > 4) return fail(TOPT_BAD_INPUT, "fem_spmv: nrhs must be 1..4");
+  if (dtype == TOPT_F64_FULL) {
+    int rc;
+    if (!h->full_ok) {
+      if (!h->full64.p &&
+          (rc = h->full64.alloc(sizeof(double) * h->ls[0].npos * h->bs * h->bs)))
+        return rc;
+      const int64_t stride0 = h->n_ke == 1 ? 0 : (int64_t)(h->bs * h->nloc) * (h->bs * h->nloc);
+      if ((rc = assemble<double>(h, h->ls[0], h->bs, h->nloc, h->ke64.as<double>(), stride0,
+                                 h->coef64.as<double>(), h->extra64, nullptr,
+                                 h->full64.as<double>())))
+        return rc;
+      h->full_ok = true;
+    }
+    return spmv<double>(h, h->ls[0], h->bs, nrhs, 0, false, h->full64.as<double>(),
+                        (const double*)x, nullptr, (double*)y);
+  }
   if (dtype == TOPT_F64)
     return spmv<double>(h, h->ls[0], h->bs, nrhs, 0, false, op64(h), (const double*)x, nullptr,
                         (double*)y);

@@ -13,11 +13,20 @@ namespace topt {
 // --------------------------------------------------------------------------
 // Material interpolation E(rho): interp 0 SIMP, Emin + (E0 - Emin) rho^p
 // (composer.py:19-22); 1 RAMP, Emin + (E0 - Emin) rho / (1 + p (1 - rho))
-// (composer.py:25-39).
+// (composer.py:25-39); 2 RAMP operator whose sensitivity keeps the SIMP form
+// (the heat plugin, solver_heat.py:928-950, calls dC_drho_simp whatever the
+// interpolation).
 __device__ __forceinline__ double interp_E(int interp, double r, double E0, double Emin,
                                            double p) {
-  if (interp == 1) return Emin + (E0 - Emin) * (r / (1.0 + p * (1.0 - r)));
+  if (interp == 1 || interp == 2) return Emin + (E0 - Emin) * (r / (1.0 + p * (1.0 - r)));
   return Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
+}
+
+__global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+  TOPT_KERNEL_COUNT();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = (float)a[i];
 }
 
 __global__ void k_simp_coef(int64_t n, const double* __restrict__ rho, double E0,
@@ -63,14 +72,16 @@ __device__ __forceinline__ int64_t vidx(int64_t p, int v) {
 // Fixed-pattern assembly: one thread per block position sums its element
 // contributions in ascending element order (deterministic, no atomics).
 // ke_stride == 0 means one matrix shared by all elements (kept in shared
-// memory).  mask (per DOF) applies skfem.enforce: rows and columns of fixed
-// DOFs are zeroed and their diagonal set to 1.
+// memory).  extra (optional, one (BS NLOC)^2 matrix per element) is added
+// unscaled: the heat plugin's Robin terms.  mask (per DOF) applies
+// skfem.enforce: rows and columns of fixed DOFs are zeroed and their
+// diagonal set to 1.
 template <typename T, int BS, int NLOC>
 __global__ void k_assemble(int64_t npos, SellT sp, const int64_t* __restrict__ cptr,
                            const int32_t* __restrict__ contrib,
                            const T* __restrict__ ke, int64_t ke_stride,
-                           const T* __restrict__ coef, const uint8_t* __restrict__ mask,
-                           T* __restrict__ vals) {
+                           const T* __restrict__ coef, const T* __restrict__ extra,
+                           const uint8_t* __restrict__ mask, T* __restrict__ vals) {
   TOPT_KERNEL_COUNT();
   constexpr int ND = BS * NLOC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -97,6 +108,14 @@ __global__ void k_assemble(int64_t npos, SellT sp, const int64_t* __restrict__ c
 #pragma unroll
         for (int d0 = 0; d0 < BS; ++d0)
           acc[c0 * BS + d0] += s * K[(BS * la + c0) * ND + BS * lb + d0];
+      if (extra) {
+        const T* X = extra + (int64_t)e * (ND * ND);
+#pragma unroll
+        for (int c0 = 0; c0 < BS; ++c0)
+#pragma unroll
+          for (int d0 = 0; d0 < BS; ++d0)
+            acc[c0 * BS + d0] += X[(BS * la + c0) * ND + BS * lb + d0];
+      }
     }
     if (mask) {
       const int64_t a = (int64_t)sp.slice_of_grp[k >> 5] * 32 + (k & 31);
@@ -1264,8 +1283,8 @@ k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
            const int32_t* __restrict__ cell_ptr,
            const int32_t* __restrict__ cell_elems, const int32_t* __restrict__ t,
            int64_t n_elem_f, const T* __restrict__ ke, int64_t ke_stride,
-           const T* __restrict__ coef, const uint8_t* __restrict__ mask,
-           T* __restrict__ kc) {
+           const T* __restrict__ coef, const T* __restrict__ extra,
+           const uint8_t* __restrict__ mask, T* __restrict__ kc) {
   TOPT_KERNEL_COUNT();
   constexpr int NF = BS * NLOC;   // fine element DOFs
   constexpr int NC = BS * 8;      // coarse cell DOFs
@@ -1286,7 +1305,7 @@ k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
   T acc[PER];
 #pragma unroll
   for (int q = 0; q < PER; ++q) acc[q] = T(0);
-  if (ke_stride == 0) {
+  if (ke_stride == 0 && !extra) {
     for (int i = threadIdx.x; i < NF * NF; i += blockDim.x) Ks[i] = ke[i];
   }
   for (int fz = az0; fz < az1; ++fz)
@@ -1298,9 +1317,15 @@ k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
         for (int64_t ei = e0; ei < e1; ++ei) {
           const int64_t e = cell_ptr ? cell_elems[ei] : ei;
           __syncthreads();
-          if (ke_stride != 0)
+          if (extra) {
+            // coef_e Ke + X_e, folded here (the scale below is then 1)
+            const T ce = coef ? coef[e] : T(1);
+            for (int i = threadIdx.x; i < NF * NF; i += blockDim.x)
+              Ks[i] = ce * ke[e * ke_stride + i] + extra[e * (NF * NF) + i];
+          } else if (ke_stride != 0) {
             for (int i = threadIdx.x; i < NF * NF; i += blockDim.x)
               Ks[i] = ke[e * ke_stride + i];
+          }
           if (threadIdx.x < NLOC * 8) {
             const int a = threadIdx.x / 8, k = threadIdx.x % 8;
             const int64_t n = t[(int64_t)a * n_elem_f + e];
@@ -1320,7 +1345,7 @@ k_galerkin(GridT g, const int32_t* __restrict__ cell_list,
             const int64_t n = t[(int64_t)a * n_elem_f + e];
             Mk[threadIdx.x] = (mask && mask[n * BS + c]) ? T(0) : T(1);
           }
-          if (threadIdx.x == 0) sc = coef ? coef[e] : T(1);
+          if (threadIdx.x == 0) sc = (coef && !extra) ? coef[e] : T(1);
           __syncthreads();
           // Tm[(a,c),(l,d)] = sum_b Ks[(a,c),(b,d)] Mk[(b,d)] W[b][l]
           for (int i = threadIdx.x; i < NF * NC; i += blockDim.x) {
@@ -1517,11 +1542,16 @@ __global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
     }
     const double h = dh ? dh[e] : 1.0;
     for (int j = 0; j < L; ++j) {
-      double u[ND];
+      // u - u(node 0) per component: a translation lies in the null space of
+      // every element matrix, and the shift keeps u^T K u from cancelling
+      // when the field carries a large offset (a prescribed temperature)
+      double u[ND], u0[BS];
+#pragma unroll
+      for (int c = 0; c < BS; ++c) u0[c] = U[(node[0] * BS + c) * L + j];
 #pragma unroll
       for (int a = 0; a < NLOC; ++a)
 #pragma unroll
-        for (int c = 0; c < BS; ++c) u[a * BS + c] = U[(node[a] * BS + c) * L + j];
+        for (int c = 0; c < BS; ++c) u[a * BS + c] = U[(node[a] * BS + c) * L + j] - u0[c];
       double q = 0.0;
 #pragma unroll
       for (int i = 0; i < ND; ++i) {

@@ -20,6 +20,7 @@ TOPT_CUDA_ERROR = 5
 TOPT_NO_MEMORY = 6
 TOPT_F64 = 0
 TOPT_F32 = 1
+TOPT_F64_FULL = 2
 TOPT_OC_EXACT = 1
 
 STATUS_NAMES = {
@@ -92,6 +93,7 @@ SIGNATURES = {
     "topt_fem_sizes": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I32)]),
     "topt_fem_update": (C.c_int, [_P, _P, _D, _D, _D]),
     "topt_fem_set_interpolation": (C.c_int, [_P, _I32]),
+    "topt_fem_set_element_extra": (C.c_int, [_P, _P]),
     "topt_fem_solve": (C.c_int, [_P, _P, _P, _I32, C.POINTER(SolveOpts),
                                  C.POINTER(SolveInfo), _P]),
     "topt_fem_spmv": (C.c_int, [_P, _I32, _P, _P, _I32]),
@@ -124,6 +126,16 @@ SIGNATURES = {
     "topt_reduce_max_abs": (C.c_int, [_I64, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot_noalloc": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
+    "topt_heat_create": (C.c_int, [_I64, _I64, _P, _P, _I32, C.POINTER(_P)]),
+    "topt_heat_destroy": (None, [_P]),
+    "topt_heat_set_stream": (C.c_int, [_P, _P]),
+    "topt_heat_set_surface": (C.c_int, [_P, _I64, _P, _P]),
+    "topt_heat_nodal_average": (C.c_int, [_P, _P, _P]),
+    "topt_heat_robin": (C.c_int, [_P, _P, _D, _D, _D, _D, _I32, _P, _P]),
+    "topt_heat_exchange": (C.c_int, [_P, _P, _P, _I32, _D, _D, C.POINTER(_D), _P]),
+    "topt_heat_exchange_adjoint": (C.c_int, [_P, _P, _D, _D, _D, _D, _D, _P]),
+    "topt_heat_robin_grad": (C.c_int, [_P, _P, _P, _I32, _D, _D, _D, _D, _P]),
+    "topt_heat_grad_dot": (C.c_int, [_P, _P, _P, _I32, _P]),
 }
 
 _lib = None

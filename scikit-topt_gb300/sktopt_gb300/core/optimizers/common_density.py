@@ -179,8 +179,12 @@ class DensityMethod:
 
     # ------------------------------------------------------------------ set-up
     def add_recorder(self, tsk):
+        """common_density.py:591-611; the objective history is named after a
+        heat task's objective (_objective_history_name 613-616)."""
+        self.objective_name = str(getattr(tsk, "objective", "compliance")) \
+            if isinstance(tsk, LinearHeatConduction) else "compliance"
         r = tools.HistoryCollection(self.cfg.dst_path)
-        for k in ("rho_projected", "energy", "vol_error", "u_max", "compliance",
+        for k in ("rho_projected", "energy", "vol_error", "u_max", self.objective_name,
                   "scaling_rate", "neumann_scale", "rho_change_max", "kkt_residual"):
             r.add(k)
         return r
@@ -350,7 +354,7 @@ class DensityMethod:
         st.rho_change_max = rcm
         rec = self.recorder
         rec.feed_data("rho_change_max", rcm)
-        rec.feed_data("compliance", compliance_avg)
+        rec.feed_data(self.objective_name, compliance_avg)
         rec.feed_data("neumann_scale", nscale)
         converged = False
         if cfg.check_convergence:

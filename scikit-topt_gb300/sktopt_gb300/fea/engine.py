@@ -92,8 +92,18 @@ class FemEngine:
         N.check(self.lib.topt_fem_set_stream(self.h, C.c_void_p(stream_handle())))
 
     def set_interpolation(self, kind: int):
-        """0 SIMP, 1 RAMP for the later update / energy calls."""
+        """0 SIMP, 1 RAMP, 2 RAMP with the SIMP-form sensitivity, for the
+        later update / energy calls."""
         N.check(self.lib.topt_fem_set_interpolation(self.h, int(kind)))
+
+    def set_extra(self, extra: torch.Tensor | None):
+        """Per-element matrices (n_e, nd, nd) added to the level-0 operator
+        from the next update on; the tensor must stay alive (None removes)."""
+        if extra is not None:
+            assert extra.is_cuda and extra.dtype == torch.float64 and extra.is_contiguous()
+        self._extra = extra
+        N.check(self.lib.topt_fem_set_element_extra(
+            self.h, C.c_void_p(extra.data_ptr()) if extra is not None else None))
 
     def update(self, rho: torch.Tensor, E0: float, Emin: float, p: float):
         """coef = SIMP(rho); K = sum coef Ke; enforce; refresh the preconditioner."""
@@ -124,11 +134,14 @@ class FemEngine:
             raise N.ToptError(info.status, f"linear solve failed: {st}")
         return comp, st
 
-    def spmv(self, x: torch.Tensor, dtype=torch.float64) -> torch.Tensor:
+    def spmv(self, x: torch.Tensor, dtype=torch.float64, full: bool = False) -> torch.Tensor:
+        """y = K x with the enforced operator, or (full) the FP64 operator
+        before Dirichlet enforcement."""
         self._bind()
         L = x.shape[1] if x.dim() == 2 else 1
         y = torch.empty_like(x)
-        code = N.TOPT_F64 if dtype == torch.float64 else N.TOPT_F32
+        code = N.TOPT_F64_FULL if full else \
+            (N.TOPT_F64 if dtype == torch.float64 else N.TOPT_F32)
         N.check(self.lib.topt_fem_spmv(self.h, code, C.c_void_p(x.data_ptr()),
                                        C.c_void_p(y.data_ptr()), L))
         return y

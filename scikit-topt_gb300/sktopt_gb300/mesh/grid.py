@@ -188,3 +188,46 @@ def setdiff1d(a, b):
     """sktopt/mesh/task_common.py:18-21."""
     a = np.asarray(a)
     return np.ascontiguousarray(a[~np.isin(a, b)])
+
+
+def get_points_in_range(x_rng, y_rng, z_rng):
+    """sktopt/mesh/utils.py:8-15: closed-box test on points (3, n)."""
+    def in_range(x):
+        return ((x[0] >= x_rng[0]) & (x[0] <= x_rng[1]) & (x[1] >= y_rng[0]) &
+                (x[1] <= y_rng[1]) & (x[2] >= z_rng[0]) & (x[2] <= z_rng[1]))
+    return in_range
+
+
+def hex_face_local_nodes(axis: int, side: int) -> list:
+    """Local nodes (MeshHex order) of the hexahedron face normal to ``axis``
+    at offset ``side`` (0 or 1)."""
+    return [a for a in range(8) if HEX_OFFSETS[a][axis] == side]
+
+
+def boundary_faces(mesh: GridMesh, predicate) -> np.ndarray:
+    """Boundary faces of a structured hex grid whose midpoints satisfy
+    ``predicate`` (scikit-fem ``Mesh.with_boundaries`` over boundary facets,
+    the tagging of sktopt's ``from_mesh_tags`` tasks, task_heat.py:252-321).
+    Rows (element, axis, side), grouped by face plane."""
+    if mesh.kind != "hex":
+        raise ValueError("boundary_faces needs a structured hex mesh")
+    n = mesh.shape
+    e = np.arange(mesh.nelements)
+    cell = (((e // n[1]) % n[0]), e % n[1], e // (n[1] * n[0]))
+    rows = []
+    for axis in range(3):
+        for side in (0, 1):
+            sel = e[cell[axis] == (0 if side == 0 else n[axis] - 1)]
+            loc = hex_face_local_nodes(axis, side)
+            mid = mesh.p[:, mesh.t[loc][:, sel]].mean(axis=1)
+            keep = sel[np.asarray(predicate(mid), dtype=bool)]
+            rows.append(np.stack([keep, np.full(keep.size, axis), np.full(keep.size, side)], 1))
+    return np.concatenate(rows).astype(np.int64)
+
+
+def face_nodes(mesh: GridMesh, faces: np.ndarray) -> np.ndarray:
+    """Sorted unique nodes of the faces (element, axis, side)."""
+    if len(faces) == 0:
+        return np.array([], dtype=np.int64)
+    return np.unique(np.concatenate([mesh.t[hex_face_local_nodes(a, s), e]
+                                     for e, a, s in faces]))

@@ -13,7 +13,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .grid import GridMesh, elements_volume, get_elements_by_nodes, setdiff1d
+from .grid import (GridMesh, boundary_faces, elements_volume, face_nodes,
+                   get_elements_by_nodes, setdiff1d)
 
 _COMP = {"u^1": 0, "u^2": 1, "u^3": 2}
 
@@ -111,24 +112,95 @@ class LinearElasticity(FEMDomain):
 
 @dataclass
 class LinearHeatConduction(FEMDomain):
+    """task_heat.py:142-321.
+
+    ``dirichlet_values``: one temperature, or a list (one load case per
+    value on the same Dirichlet nodes).  ``emit``: optional volumetric
+    source (nodal load; the reference has none).  Robin data
+    (task_common.py:76-81): ``robin_faces`` -- an (n, 3) array of hexahedron
+    faces (element, axis, side) or a list of such groups -- with
+    ``robin_coefficient`` h and ``robin_bc_value`` T_env (scalars, or one per
+    group for the surface terms).  ``objective``: "compliance",
+    "heat_exchange" or "averaged_temp"."""
     k: float = 1.0
-    dirichlet_values: float = 0.0
+    dirichlet_values: float | list = 0.0
     emit: np.ndarray | None = None
     objective: str = "compliance"
+    robin_faces: np.ndarray | list | None = None
+    robin_coefficient: float | list | None = None
+    robin_bc_value: float | list | None = None
+    design_robin_boundary: bool | None = None
+    robin_elements: np.ndarray | None = None
+    avg_temp_weight: float = 0.0
 
     @property
     def material_coef(self) -> float:
         return self.k
 
     @property
+    def dirichlet_value_list(self) -> list:
+        v = self.dirichlet_values
+        return [float(x) for x in v] if isinstance(v, (list, tuple)) else [float(v)]
+
+    @property
     def n_tasks(self) -> int:
-        return 1
+        return len(self.dirichlet_value_list)
+
+    @property
+    def robin_groups(self) -> list:
+        if self.robin_faces is None:
+            return []
+        g = self.robin_faces if isinstance(self.robin_faces, list) else [self.robin_faces]
+        return [np.asarray(x, dtype=np.int64).reshape(-1, 3) for x in g]
 
     @classmethod
     def from_nodes(cls, mesh, dirichlet_nodes, emit, design_elements, k=1.0,
-                   dirichlet_values=0.0):
-        """task_heat.py:142-321 with a volumetric source vector ``emit``."""
+                   dirichlet_values=0.0, robin_faces=None, robin_coefficient=None,
+                   robin_bc_value=None, design_robin_boundary=None,
+                   objective="compliance", avg_temp_weight=0.0):
+        """task_heat.py:172-250 and task_common.py:105-270: elements touching
+        Robin facets leave the design set when design_robin_boundary is False."""
+        if objective not in ("compliance", "heat_exchange", "averaged_temp"):
+            raise ValueError("objective must be one of 'compliance', 'heat_exchange', "
+                             "or 'averaged_temp'")
         s = FEMDomain._sets(mesh, 1, dirichlet_nodes, "all", None, design_elements)
+        rob_el = None
+        if robin_faces is not None:
+            groups = robin_faces if isinstance(robin_faces, list) else [robin_faces]
+            allf = np.concatenate([np.asarray(g, dtype=np.int64).reshape(-1, 3)
+                                   for g in groups])
+            rob_el = np.unique(allf[:, 0])
+            if design_robin_boundary is False:
+                s["design_elements"] = setdiff1d(s["design_elements"], rob_el)
+                s["fixed_elements"] = setdiff1d(s["all_elements"], s["design_elements"])
+        if emit is None:
+            emit = np.zeros(mesh.nnodes)
         return cls(mesh=mesh, neumann_nodes=None, bs=1, k=float(k),
-                   dirichlet_values=float(dirichlet_values),
-                   emit=np.ascontiguousarray(emit, dtype=np.float64), **s)
+                   dirichlet_values=dirichlet_values,
+                   emit=np.ascontiguousarray(emit, dtype=np.float64), objective=objective,
+                   robin_faces=robin_faces, robin_coefficient=robin_coefficient,
+                   robin_bc_value=robin_bc_value, design_robin_boundary=design_robin_boundary,
+                   robin_elements=rob_el, avg_temp_weight=float(avg_temp_weight), **s)
+
+    @classmethod
+    def from_boundaries(cls, mesh, dirichlet, dirichlet_values, robin, robin_coefficient,
+                        robin_bc_value, design_robin_boundary, k,
+                        objective="compliance", avg_temp_weight=0.0, design_elements=None,
+                        emit=None):
+        """task_heat.py:252-321 with boundary predicates in place of mesh tags:
+        ``dirichlet`` / ``robin`` are point predicates (get_points_in_range)
+        or lists of them, applied to boundary-facet midpoints."""
+        dl = dirichlet if isinstance(dirichlet, list) else [dirichlet]
+        dn = np.unique(np.concatenate([face_nodes(mesh, boundary_faces(mesh, f)) for f in dl]))
+        rob = None
+        if robin is not None:
+            rl = robin if isinstance(robin, list) else [robin]
+            rob = [boundary_faces(mesh, f) for f in rl]
+        if design_elements is None:
+            design_elements = np.arange(mesh.nelements)
+        return cls.from_nodes(mesh, dn, emit, design_elements, k=k,
+                              dirichlet_values=dirichlet_values, robin_faces=rob,
+                              robin_coefficient=robin_coefficient,
+                              robin_bc_value=robin_bc_value,
+                              design_robin_boundary=design_robin_boundary,
+                              objective=objective, avg_temp_weight=avg_temp_weight)

@@ -1,0 +1,145 @@
+"""CPU checks of the oracle's heat Robin / heat-exchange restatement
+(oracle/heat_robin.py) against analytic identities, and of the task set-up.
+
+* the 2x2x2 rule integrates |grad rho| of a linear nodal field exactly
+  (|a| x volume) and the virtual Robin terms vanish (to rounding) for a
+  uniform density;
+* surface Robin matrices sum to h x area and their loads to h T_env x area;
+* the explicit Robin gradient is the derivative, at fixed T, of
+  G(rho) = int h rho^p (1 - rho)^q |grad rho| (2 T_env T - T^2)
+  (central differences, 1e-6 relative);
+* the reference's nodal-average pairing differs from the element pairing
+  and both reproduce a uniform density;
+* without Robin data and with T = 0 Dirichlet values the compliance
+  objective equals the plain conduction problem's;
+* the plate task's Dirichlet nodes and Robin facets match the oracle's.
+"""
+import numpy as np
+import pytest
+
+from oracle import fem as ofem
+from oracle import heat_robin as hr
+from oracle import problems
+
+
+def _plate(n=(6, 6, 2)):
+    return problems.heat_plate(*n)
+
+
+def test_linear_field_interface_integral_exact():
+    m, pb, *_ = _plate()
+    a = np.array([0.3, -0.2, 0.5])
+    rho_n = 0.1 + a @ m.p * 0.01
+    vol = 8.0 * 8.0 * 1.0
+    den = hr.hx_den(m, pb.Q, rho_n)
+    assert abs(den - 0.01 * np.linalg.norm(a) * vol) <= 1e-13 * den
+
+
+def test_virtual_robin_vanishes_for_uniform_density():
+    m, pb, *_ = _plate()
+    Me, fe = hr.virtual_robin(m, pb.Q, np.full(m.nnodes, 0.4), 4e-5, 300.0, 3.0, 4.0)
+    # |grad rho| of a constant field is rounding noise (~1e-17), not zero
+    assert np.abs(Me).max() <= 1e-20 and np.abs(fe).max() <= 1e-17
+
+
+def test_surface_robin_sums():
+    m, pb, *_ = _plate((5, 4, 3))
+    faces = problems.boundary_faces(m, problems.in_range((0, 0), (0, 8), (0, 1)))
+    Me, load = hr.surface_robin(m, faces, 2.0, 300.0)
+    area = 8.0 * 1.0
+    assert abs(Me.sum() - 2.0 * area) <= 1e-12 * area
+    assert abs(load.sum() - 2.0 * 300.0 * area) <= 1e-10 * area
+    for M in Me:
+        assert np.allclose(M, M.T, rtol=0, atol=1e-15)
+
+
+def test_explicit_robin_gradient_finite_differences():
+    m, pb, *_ = _plate((4, 4, 2))
+    rng = np.random.default_rng(7)
+    rho_n = rng.uniform(0.2, 0.8, m.nnodes)
+    T = rng.uniform(250.0, 650.0, m.nnodes)
+    h, te, p, q = 4e-5, 300.0, 3.0, 4.0
+    N, dN, wd = pb.Q
+
+    def G(r):
+        rq, g = hr._at_qp(N, dN, m, r)
+        tq, _ = hr._at_qp(N, dN, m, T)
+        iface = np.sqrt(np.sum(g ** 2, axis=2))
+        return float(np.sum(wd * h * rq ** p * (1 - rq) ** q * iface * (2 * te * tq - tq * tq)))
+
+    grad = hr.robin_explicit_grad(m, pb.Q, rho_n, T, h, te, p, q)
+    for n in rng.choice(m.nnodes, 6, replace=False):
+        e = np.zeros(m.nnodes)
+        e[n] = 1e-6
+        fd = (G(rho_n + e) - G(rho_n - e)) / 2e-6
+        assert abs(fd - grad[n]) <= 1e-6 * max(abs(grad).max(), 1e-300), (n, fd, grad[n])
+
+
+def test_nodal_average_pairings():
+    m, *_ = _plate((4, 3, 2))
+    rng = np.random.default_rng(3)
+    rho = rng.uniform(0, 1, m.nelements)
+    ref, cnt = hr.nodal_average(m, rho, "reference")
+    ele, cnt2 = hr.nodal_average(m, rho, "element")
+    assert np.array_equal(cnt, cnt2)
+    assert not np.allclose(ref, ele)
+    # element pairing: the plain average over the node's elements
+    want = np.zeros(m.nnodes)
+    for e in range(m.nelements):
+        want[m.t[:, e]] += rho[e]
+    np.testing.assert_allclose(ele, want / cnt, rtol=1e-14)
+    u = np.full(m.nelements, 0.37)
+    np.testing.assert_allclose(hr.nodal_average(m, u, "reference")[0], 0.37, rtol=1e-15)
+
+
+def test_no_robin_zero_dirichlet_matches_plain_conduction():
+    m, pb, *_ = problems.heat_plate(10, 10, 2, dirichlet_values=0.0, robin=False)
+    assert pb.D.size > 0
+    emit = ofem.source_vector(m, 1.0)
+    pb.emit = emit
+    plain = ofem.HeatProblem(m, pb.D, k0=10.0, emit=emit)
+    rho = np.random.default_rng(1).uniform(0.1, 1.0, m.nelements)
+    J, T = pb.objectives(rho, 3.0, 1e-2)
+    J0, T0 = plain.objectives(rho, 3.0, 1e-2)
+    assert abs(J[0] - J0[0]) <= 1e-12 * abs(J0[0])
+    np.testing.assert_allclose(T, T0, rtol=0, atol=1e-12 * np.abs(T0).max())
+
+
+def test_plate_task_matches_oracle_sets():
+    from sktopt_gb300.mesh import toy_problem
+    t = toy_problem.heat_plate(10, 9, 3)
+    m, pb, design, fixed, vol = problems.heat_plate(10, 9, 3)
+    assert np.array_equal(t.mesh.t, m.t) and np.allclose(t.mesh.p, m.p, rtol=0, atol=1e-15)
+    assert np.array_equal(np.sort(t.dirichlet_nodes), pb.D)
+    got = [np.asarray(g) for g in t.robin_groups]
+    want = [problems.boundary_faces(m, problems.in_range((0, 0), (0, 8), (0, 1))),
+            problems.boundary_faces(m, problems.in_range((0, 8), (8, 8), (0, 1)))]
+    for a, b in zip(got, want):
+        assert np.array_equal(a, b)
+    t.exlude_dirichlet_from_design()
+    assert np.array_equal(np.sort(t.design_elements), np.sort(design))
+
+
+def test_surface_matrices_match_oracle():
+    from sktopt_gb300.fea.solver_heat import surface_robin_load, surface_robin_matrices
+    from sktopt_gb300.mesh import toy_problem
+    t = toy_problem.heat_plate(5, 4, 3)
+    m, *_ = problems.heat_plate(5, 4, 3)
+    for faces in t.robin_groups:
+        Me, load = hr.surface_robin(m, faces, 4e-5, 300.0)
+        np.testing.assert_allclose(surface_robin_matrices(t.mesh, faces, 4e-5).reshape(-1, 8, 8),
+                                   Me, rtol=1e-13, atol=1e-20)
+        np.testing.assert_allclose(surface_robin_load(t.mesh, faces, 4e-5, 300.0), load,
+                                   rtol=1e-13, atol=1e-18)
+
+
+@pytest.mark.parametrize("objective", ["compliance", "heat_exchange", "averaged_temp"])
+def test_oracle_objectives_run(objective):
+    m, pb, *_ = problems.heat_plate(10, 10, 2, objective=objective, avg_temp_weight=0.5)
+    assert pb.D.size > 0
+    rho = np.random.default_rng(2).uniform(0.1, 1.0, m.nelements)
+    J, T = pb.objectives(rho, 3.0, 1e-2)
+    assert np.all(np.isfinite(J)) and np.all(np.isfinite(T))
+    assert np.abs(T[pb.D] - 600.0).max() == 0.0
+    g = pb.custom_sensitivity(rho, 3.0, 1e-2, T)
+    assert g.shape == (m.nelements, 1) and np.all(np.isfinite(g))
