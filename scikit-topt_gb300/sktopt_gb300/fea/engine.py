@@ -47,8 +47,11 @@ class FemEngine:
         self._t = np.ascontiguousarray(mesh.t, dtype=np.int32)
         self._ke = ke
         self._mask = np.ascontiguousarray(dirichlet_mask, dtype=np.uint8)
-        self._ijk = np.ascontiguousarray(mesh.node_ijk, dtype=np.int32)
-        self._cell = np.ascontiguousarray(mesh.cell_of_elem, dtype=np.int32)
+        # meshes without a logical grid (read from files) run block Jacobi
+        multigrid = multigrid and getattr(mesh, "has_grid", True)
+        if multigrid:
+            self._ijk = np.ascontiguousarray(mesh.node_ijk, dtype=np.int32)
+            self._cell = np.ascontiguousarray(mesh.cell_of_elem, dtype=np.int32)
         d = N.FemDesc()
         d.bs = bs
         d.nloc = self.nloc

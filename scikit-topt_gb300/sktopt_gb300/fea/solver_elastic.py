@@ -77,10 +77,12 @@ class LinearSolverConfig:
             return min(self.rtol, self.direct_rtol)
         return self.rtol
 
-    def resolved_maxiter(self, n_dof: int) -> int:
+    def resolved_maxiter(self, n_dof: int, multigrid: bool = True) -> int:
+        """``multigrid`` False: the engine runs block Jacobi (a mesh without
+        a logical grid) whatever the configured preconditioner."""
         if self.maxiter is not None:
             return int(self.maxiter)
-        if self.resolved_precond() == "jacobi":
+        if self.resolved_precond() == "jacobi" or not multigrid:
             # solver_elastic.py:201-204 rule, kept for the Jacobi-preconditioned path
             return min(1000, max(300, n_dof // 5)) if self.solver == "cg_jacobi" else 20000
         return 2000
@@ -165,7 +167,8 @@ class FEM_SimpLinearElasticity:
             {"fcg": 3, "replace": 4, "reliable": 1, "restart": 2}[cfg.refine]
         precond = 1 if eng.multigrid else 0
         comp, st = eng.solve(F, U, method, precond, cfg.resolved_rtol(),
-                             cfg.resolved_maxiter(eng.n_dof), cfg.inner_rtol, cfg.max_outer,
+                             cfg.resolved_maxiter(eng.n_dof, eng.multigrid), cfg.inner_rtol,
+                             cfg.max_outer,
                              cfg.cheb_degree, cfg.check_every,
                              cheb_ratio=cfg.cheb_ratio, x0=cfg.warm_start)
         self.last_stats = st

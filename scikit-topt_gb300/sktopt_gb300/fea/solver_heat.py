@@ -298,7 +298,7 @@ class FEM_SimpLinearHeatConduction:
                     self._X[k] = torch.zeros_like(Fb)
             X = self._X[k]
             _, st = eng.solve(Fb, X, method, 1 if eng.multigrid else 0, cfg.resolved_rtol(),
-                              cfg.resolved_maxiter(n), cfg.inner_rtol, cfg.max_outer,
+                              cfg.resolved_maxiter(n, eng.multigrid), cfg.inner_rtol, cfg.max_outer,
                               cfg.cheb_degree, cfg.check_every, cheb_ratio=cfg.cheb_ratio,
                               x0=cfg.warm_start)
             self.last_stats = st

@@ -20,15 +20,29 @@ TET_AXIS_ORDERS = ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1,
 
 
 class GridMesh:
-    """skfem-shaped mesh: ``p`` (3, n_nodes), ``t`` (nloc, n_elem)."""
+    """skfem-shaped mesh: ``p`` (3, n_nodes), ``t`` (nloc, n_elem).
 
-    def __init__(self, p, t, kind, shape, node_ijk, cell_of_elem):
+    Meshes read from files carry no logical grid (``shape`` None): they are
+    solved without the geometric multigrid.  ``boundaries`` (name -> facets,
+    rows (element, local face)) and ``subdomains`` (name -> elements) hold
+    the tags of a mesh file."""
+
+    def __init__(self, p, t, kind, shape=None, node_ijk=None, cell_of_elem=None,
+                 boundaries=None, subdomains=None):
         self.p = np.ascontiguousarray(p, dtype=np.float64)
         self.t = np.ascontiguousarray(t, dtype=np.int64)
         self.kind = kind
-        self.shape = tuple(int(s) for s in shape)
-        self.node_ijk = np.ascontiguousarray(node_ijk, dtype=np.int64)
-        self.cell_of_elem = np.ascontiguousarray(cell_of_elem, dtype=np.int64)
+        self.shape = tuple(int(s) for s in shape) if shape is not None else None
+        self.node_ijk = np.ascontiguousarray(node_ijk, dtype=np.int64) \
+            if node_ijk is not None else None
+        self.cell_of_elem = np.ascontiguousarray(cell_of_elem, dtype=np.int64) \
+            if cell_of_elem is not None else None
+        self.boundaries = dict(boundaries or {})
+        self.subdomains = dict(subdomains or {})
+
+    @property
+    def has_grid(self) -> bool:
+        return self.shape is not None and self.node_ijk is not None
 
     @property
     def nnodes(self) -> int:
@@ -231,3 +245,51 @@ def face_nodes(mesh: GridMesh, faces: np.ndarray) -> np.ndarray:
         return np.array([], dtype=np.int64)
     return np.unique(np.concatenate([mesh.t[hex_face_local_nodes(a, s), e]
                                      for e, a, s in faces]))
+
+
+# Local faces: hexahedron face f = 2 axis + side (the face normal to ``axis``
+# at offset ``side``); tetrahedron face f = the face opposite local node f.
+HEX_FACES = [[a for a in range(8) if HEX_OFFSETS[a][f // 2] == f % 2] for f in range(6)]
+TET_FACES = [[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]]
+
+
+def element_faces(kind: str) -> list:
+    return HEX_FACES if kind == "hex" else TET_FACES
+
+
+def facet_nodes_of(mesh: GridMesh, facets: np.ndarray) -> np.ndarray:
+    """(n, k) nodes of facets given as rows (element, local face)."""
+    faces = element_faces(mesh.kind)
+    facets = np.asarray(facets, dtype=np.int64).reshape(-1, 2)
+    if facets.shape[0] == 0:
+        return np.zeros((0, len(faces[0])), dtype=np.int64)
+    loc = np.asarray(faces)[facets[:, 1]]                       # (n, k)
+    return mesh.t[loc, facets[:, 0][:, None]]
+
+
+def boundary_facets(mesh: GridMesh, predicate=None) -> np.ndarray:
+    """Boundary facets (faces of exactly one element) as rows (element, local
+    face), in element order; with ``predicate`` only those whose midpoints
+    satisfy it (scikit-fem ``Mesh.with_boundaries`` semantics)."""
+    faces = element_faces(mesh.kind)
+    ne = mesh.nelements
+    keys, owner = [], []
+    for f, loc in enumerate(faces):
+        keys.append(np.sort(mesh.t[loc].T, axis=1))
+        owner.append(np.stack([np.arange(ne), np.full(ne, f)], 1))
+    keys = np.concatenate(keys)
+    owner = np.concatenate(owner)
+    _, inv, cnt = np.unique(keys, axis=0, return_inverse=True, return_counts=True)
+    bnd = owner[cnt[inv.reshape(-1)] == 1]
+    order = np.lexsort((bnd[:, 1], bnd[:, 0]))
+    bnd = bnd[order]
+    if predicate is not None:
+        mid = mesh.p[:, facet_nodes_of(mesh, bnd)].mean(axis=2)
+        bnd = bnd[np.asarray(predicate(mid), dtype=bool)]
+    return bnd.astype(np.int64)
+
+
+def facets_to_faces(facets: np.ndarray) -> np.ndarray:
+    """Hexahedron facets (element, f) as (element, axis, side) rows."""
+    facets = np.asarray(facets, dtype=np.int64).reshape(-1, 2)
+    return np.stack([facets[:, 0], facets[:, 1] // 2, facets[:, 1] % 2], 1)

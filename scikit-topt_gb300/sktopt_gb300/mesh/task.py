@@ -55,13 +55,20 @@ class FEMDomain:
 
     @staticmethod
     def _sets(mesh, bs, dirichlet_nodes, dirichlet_dir, neumann_nodes, design_elements):
-        dn = np.unique(np.asarray(dirichlet_nodes, dtype=np.int64))
-        if dirichlet_dir == "all" or bs == 1:
-            comps = np.arange(bs)
+        """task_common.py:105-270.  ``dirichlet_nodes`` may be a list of node
+        sets with a list of directions (one per set, task_common.py:140-160)."""
+        if isinstance(dirichlet_nodes, list):
+            dirs = dirichlet_dir if isinstance(dirichlet_dir, list) else \
+                [dirichlet_dir] * len(dirichlet_nodes)
+            parts = [FEMDomain._dofs(bs, n, d) for n, d in zip(dirichlet_nodes, dirs)]
+            ddofs = np.unique(np.concatenate(parts)) if parts else np.array([], np.int64)
+            dn = np.unique(np.concatenate([np.asarray(n, dtype=np.int64).ravel()
+                                           for n in dirichlet_nodes])) \
+                if dirichlet_nodes else np.array([], np.int64)
         else:
-            comps = np.array([_COMP[dirichlet_dir]])
-        ddofs = np.sort((bs * dn[:, None] + comps[None, :]).ravel())
-        dir_el = get_elements_by_nodes(mesh, [dn])
+            dn = np.unique(np.asarray(dirichlet_nodes, dtype=np.int64))
+            ddofs = FEMDomain._dofs(bs, dn, dirichlet_dir)
+        dir_el = get_elements_by_nodes(mesh, [dn]) if dn.size else np.array([], np.int32)
         if neumann_nodes is not None:
             nn = neumann_nodes if isinstance(neumann_nodes, list) else [neumann_nodes]
             neu_el = get_elements_by_nodes(mesh, nn)
@@ -82,6 +89,91 @@ class FEMDomain:
                     all_elements=all_el, fixed_elements=fixed,
                     dirichlet_neumann_elements=dn_el,
                     elements_volume=elements_volume(mesh))
+
+
+    @staticmethod
+    def _dofs(bs, nodes, direction):
+        nodes = np.unique(np.asarray(nodes, dtype=np.int64))
+        comps = np.arange(bs) if (direction in (None, "all") or bs == 1) else \
+            np.array([_COMP[direction]])
+        return np.sort((bs * nodes[:, None] + comps[None, :]).ravel())
+
+
+def _group_list(x):
+    return x if isinstance(x, list) else [x]
+
+
+def _tag_groups(tags: dict, prefix: str):
+    """Facet groups named ``prefix_<k>`` in k order, else ``prefix``
+    (the key rules of from_mesh_tags, task_elastic.py:266-317)."""
+    import re
+    keys = sorted([k for k in tags if re.match(rf"{prefix}_\d+$", k)],
+                  key=lambda x: int(re.search(r"\d+$", x).group()))
+    if keys:
+        return [tags[k] for k in keys]
+    if prefix in tags:
+        return [tags[prefix]]
+    return None
+
+
+def _facet_integrals(mesh, facets):
+    """Area and int N_a over each facet (rows (element, local face)): 2x2
+    Gauss on the bilinear map of a hexahedron face, exact for a triangle."""
+    from .grid import HEX_OFFSETS, element_faces
+    faces = element_faces(mesh.kind)
+    facets = np.asarray(facets, dtype=np.int64).reshape(-1, 2)
+    k = len(faces[0])
+    nodes = np.zeros((facets.shape[0], k), dtype=np.int64)
+    area = np.zeros(facets.shape[0])
+    integ = np.zeros((facets.shape[0], k))
+    g = 0.5 / np.sqrt(3.0)
+    gp = (0.5 - g, 0.5 + g)
+    for i, (e, f) in enumerate(facets):
+        loc = faces[f]
+        nodes[i] = mesh.t[loc, e]
+        X = mesh.p[:, nodes[i]]
+        if mesh.kind == "hex":
+            ax = [d for d in range(3) if d != f // 2]
+            uv = HEX_OFFSETS[loc][:, ax]
+            for s_ in gp:
+                for t_ in gp:
+                    Nf = np.array([(s_ if o[0] else 1 - s_) * (t_ if o[1] else 1 - t_)
+                                   for o in uv])
+                    dS = np.array([(1.0 if o[0] else -1.0) * (t_ if o[1] else 1 - t_)
+                                   for o in uv])
+                    dT = np.array([(s_ if o[0] else 1 - s_) * (1.0 if o[1] else -1.0)
+                                   for o in uv])
+                    jac = np.linalg.norm(np.cross(X @ dS, X @ dT))
+                    area[i] += 0.25 * jac
+                    integ[i] += 0.25 * jac * Nf
+        else:
+            a = 0.5 * np.linalg.norm(np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]))
+            area[i] = a
+            integ[i] = a / 3.0
+    return nodes, area, integ
+
+
+def assemble_surface_forces(mesh, force_facets, force_dir_type, force_value) -> list:
+    """task_elastic.py:15-81: for each facet group, a uniform traction of
+    value / (group area) along component u^1..u^3, integrated against the
+    shape functions; one load vector (3 n_nodes) per group."""
+    facets_list = _group_list(force_facets)
+    dirs = _group_list(force_dir_type)
+    vals = _group_list(force_value)
+    if not (len(facets_list) == len(dirs) == len(vals)):
+        raise ValueError("Lengths of force_facets_ids, force_dir_type, and force_value "
+                         "must match when lists.")
+    out = []
+    for fac, d, v in zip(facets_list, dirs, vals):
+        if not (isinstance(d, str) and d.startswith("u^") and d[2:].isdigit()):
+            raise ValueError(f"force_dir_type must be like 'u^1','u^2','u^3', got: {d}")
+        comp = int(d[2:]) - 1
+        nodes, area, integ = _facet_integrals(mesh, fac)
+        pressure = float(v) / float(np.sum(area))
+        F = np.zeros(3 * mesh.nnodes)
+        np.add.at(F, 3 * nodes.ravel() + comp, (pressure * integ).ravel())
+        out.append(F)
+    return out
 
 
 @dataclass
@@ -108,6 +200,41 @@ class LinearElasticity(FEMDomain):
         loads = [np.ascontiguousarray(f, dtype=np.float64) for f in loads]
         return cls(mesh=mesh, neumann_nodes=neumann_nodes, bs=3, E=float(E), nu=float(nu),
                    neumann_linear=loads, **s)
+
+    @classmethod
+    def from_facets(cls, mesh, dirichlet_facets, dirichlet_dir, force_facets, force_dir_type,
+                    force_value, design_elements, E, nu):
+        """task_elastic.py:152-258 and task_common.py:273-347: Dirichlet nodes
+        from the facets (one node set per facet group), force nodes from the
+        force facets (their elements leave the design set), and one surface
+        load vector per force group (assemble_surface_forces)."""
+        from .grid import facet_nodes_of
+        if isinstance(dirichlet_facets, list):
+            dn = [np.unique(facet_nodes_of(mesh, f)) for f in dirichlet_facets]
+        else:
+            dn = np.unique(facet_nodes_of(mesh, dirichlet_facets))
+        ff = np.concatenate([np.asarray(f, dtype=np.int64).reshape(-1, 2)
+                             for f in _group_list(force_facets)])
+        nn = np.unique(facet_nodes_of(mesh, ff))
+        loads = assemble_surface_forces(mesh, force_facets, force_dir_type, force_value)
+        return cls.from_nodes(mesh, dn, dirichlet_dir, nn, loads, design_elements, E, nu)
+
+    @classmethod
+    def from_mesh_tags(cls, mesh, dirichlet_dir, neumann_dir_type, neumann_values, E, nu):
+        """task_elastic.py:266-317: facet groups ``dirichlete_<k>`` (the
+        reference's spelling) or ``dirichlet``, ``neumann_<k>`` or ``neumann``,
+        design elements from the ``design`` subdomain."""
+        design = mesh.subdomains["design"]
+        dir_f = _tag_groups(mesh.boundaries, "dirichlete")
+        if dir_f is None:
+            dir_f = [mesh.boundaries["dirichlet"]] if "dirichlet" in mesh.boundaries else []
+        if len(dir_f) == 1 and not isinstance(dirichlet_dir, list):
+            dir_f = dir_f[0]
+        neu_f = _tag_groups(mesh.boundaries, "neumann") or []
+        if len(neu_f) == 1 and not isinstance(neumann_dir_type, list):
+            neu_f = neu_f[0]
+        return cls.from_facets(mesh, dir_f, dirichlet_dir, neu_f, neumann_dir_type,
+                               neumann_values, design, E, nu)
 
 
 @dataclass
@@ -181,6 +308,39 @@ class LinearHeatConduction(FEMDomain):
                    robin_faces=robin_faces, robin_coefficient=robin_coefficient,
                    robin_bc_value=robin_bc_value, design_robin_boundary=design_robin_boundary,
                    robin_elements=rob_el, avg_temp_weight=float(avg_temp_weight), **s)
+
+    @classmethod
+    def from_facets(cls, mesh, dirichlet_facets, dirichlet_values, robin_facets,
+                    robin_coefficient, robin_bc_value, design_robin_boundary, design_elements,
+                    k, objective="compliance", avg_temp_weight=0.0, emit=None):
+        """task_heat.py:172-250 with facets as rows (element, local face);
+        Robin facets must be hexahedron faces."""
+        from .grid import facet_nodes_of, facets_to_faces
+        groups = _group_list(dirichlet_facets)
+        dn = np.unique(np.concatenate([facet_nodes_of(mesh, f).ravel() for f in groups]))
+        rob = None
+        if robin_facets is not None:
+            if mesh.kind != "hex":
+                raise NotImplementedError("Robin facets need a hexahedral mesh")
+            rob = [facets_to_faces(f) for f in _group_list(robin_facets)]
+        return cls.from_nodes(mesh, dn, emit, design_elements, k=k,
+                              dirichlet_values=dirichlet_values, robin_faces=rob,
+                              robin_coefficient=robin_coefficient,
+                              robin_bc_value=robin_bc_value,
+                              design_robin_boundary=design_robin_boundary,
+                              objective=objective, avg_temp_weight=avg_temp_weight)
+
+    @classmethod
+    def from_mesh_tags(cls, mesh, dirichlet_values, robin_coefficient, robin_bc_value,
+                       design_robin_boundary, k, objective="compliance", avg_temp_weight=0.0):
+        """task_heat.py:252-321: ``dirichlet_<k>`` / ``dirichlet`` and
+        ``robin_<k>`` / ``robin`` facet groups, the ``design`` subdomain."""
+        dir_f = _tag_groups(mesh.boundaries, "dirichlet")
+        rob_f = _tag_groups(mesh.boundaries, "robin")
+        return cls.from_facets(mesh, dir_f, dirichlet_values, rob_f, robin_coefficient,
+                               robin_bc_value, design_robin_boundary,
+                               mesh.subdomains["design"], k, objective=objective,
+                               avg_temp_weight=avg_temp_weight)
 
     @classmethod
     def from_boundaries(cls, mesh, dirichlet, dirichlet_values, robin, robin_coefficient,
