@@ -82,3 +82,54 @@ class BatchedDesigns:
 
     def __len__(self):
         return len(self.opts)
+
+
+def partition_designs(costs, world_size: int) -> list:
+    """Split designs over ``world_size`` ranks, balancing the summed cost
+    (e.g. element or nonzero counts): largest first onto the least loaded
+    rank, ties to the lower rank; each rank's list in ascending design order.
+    Deterministic, so every rank computes the same partition without a
+    collective."""
+    costs = np.asarray(costs, dtype=np.float64)
+    load = np.zeros(world_size)
+    parts = [[] for _ in range(world_size)]
+    for i in np.argsort(-costs, kind="stable"):
+        r = int(np.argmin(load))
+        parts[r].append(int(i))
+        load[r] += costs[i]
+    return [sorted(p) for p in parts]
+
+
+def gather_design_results(local: dict, group=None) -> dict | None:
+    """The one collective of a sharded batch: every rank's {design index:
+    result} is gathered on rank 0 (None elsewhere); a single process
+    returns its own results."""
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return dict(local)
+    world = dist.get_world_size(group)
+    out = [None] * world if dist.get_rank(group) == 0 else None
+    dist.gather_object(local, out, dst=0, group=group)
+    if out is None:
+        return None
+    merged = {}
+    for part in out:
+        merged.update(part)
+    return merged
+
+
+def run_sharded(makers, costs, steps: int, rank: int = 0, world_size: int = 1,
+                n_workers: int = 8, device=None, result=None):
+    """Run this rank's share of a batch of designs (``partition_designs``)
+    for ``steps`` OC iterations and gather the per-design results on rank 0.
+    ``result(opt)`` extracts what is gathered (default: the objective
+    history)."""
+    mine = partition_designs(costs, world_size)[rank]
+    local = {}
+    if mine:
+        batch = BatchedDesigns([makers[i] for i in mine], n_workers=n_workers, device=device)
+        batch.step(steps)
+        for i, opt in zip(mine, batch.opts):
+            local[i] = result(opt) if result else \
+                list(opt.recorder.histories[getattr(opt, "objective_name", "compliance")])
+    return gather_design_results(local)

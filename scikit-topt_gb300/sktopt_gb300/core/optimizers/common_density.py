@@ -101,6 +101,9 @@ class DensityMethodConfig:
     # edge (same result as the all-FP64 bisection); False = FP64 every step
     bisection_fp32_bracket: bool = True
     export: bool = False
+    # with export: the VTU of each saved iteration (mesh_rho/info_mesh-*.vtu)
+    # and cubic_top.vtu at the end, as the reference writes them
+    export_vtu: bool = True
 
     @classmethod
     def from_defaults(cls, **args):
@@ -111,6 +114,10 @@ class DensityMethodConfig:
         self.solver_config = normalize_linear_solver_config(
             self.solver_option, rtol=self.solver_rtol, precision=self.precision,
             precond=self.precond, inner_rtol=self.inner_rtol)
+
+    def vtu_path(self, iter_num: int):
+        """common_density.py:338-339."""
+        return f"{self.dst_path}/mesh_rho/info_mesh-{iter_num:08d}.vtu"
 
     def export_cfg(self, path: str):
         d = {k: (asdict(v) if hasattr(v, "__dataclass_fields__") else v)
@@ -142,7 +149,9 @@ class DensityMethod:
         if cfg.export:
             os.makedirs(cfg.dst_path, exist_ok=True)
             os.makedirs(f"{cfg.dst_path}/data", exist_ok=True)
+            os.makedirs(f"{cfg.dst_path}/mesh_rho", exist_ok=True)
             cfg.export_cfg(cfg.dst_path)
+        self._snap = None
         if cfg.design_dirichlet is False:
             tsk.exlude_dirichlet_from_design()
         # common_density.py:392-404 (interpolation_funcs)
@@ -294,13 +303,20 @@ class DensityMethod:
             self._finalize()
             return
         it1 = st.iter_end if max_steps is None else min(it0 + max_steps, st.iter_end)
+        try:
+            self._run_steps(it0, it1)
+        finally:
+            if self._snap is not None:
+                self._snap.flush()
+        if self._iter_next >= st.iter_end:
+            self._finalize()
+
+    def _run_steps(self, it0, it1):
         for it in range(it0, it1):
             converged = self.step(it)
             self._iter_next = it + 1
             if converged:
                 break
-        if self._iter_next >= st.iter_end:
-            self._finalize()
 
     def scheduled_values(self, it):
         return self.schedulers.values_as_list(
@@ -366,10 +382,28 @@ class DensityMethod:
             rec_every = max(cfg.max_iters // cfg.record_times, 1)
             if iter_num % rec_every == 0 or iter_num == 1 or converged or \
                     iter_num == st.iter_end - 1:
-                d = st.rho[self.design].cpu().numpy()
-                np.savez_compressed(f"{cfg.dst_path}/data/{iter_num:06d}-rho.npz",
-                                    rho_design_elements=d)
+                self._export_iteration(iter_num, st)
         return converged
+
+    def _export_iteration(self, iter_num, st):
+        """common_density.py:1186-1233: data/NNNNNN-rho.npz and the VTU with
+        rho_projected and energy, written off the compute stream."""
+        from ..snapshot import SnapshotWriter
+        from ..visualization import export_mesh_with_info
+        cfg, tsk = self.cfg, self.tsk
+        if self._snap is None:
+            self._snap = SnapshotWriter(self.device)
+        design = np.asarray(tsk.design_elements)
+
+        def write(h):
+            np.savez_compressed(f"{cfg.dst_path}/data/{iter_num:06d}-rho.npz",
+                                rho_design_elements=h["rho"][design])
+            if cfg.export_vtu:
+                export_mesh_with_info(tsk.mesh, cell_data_names=["rho_projected", "energy"],
+                                      cell_data_values=[h["rho_projected"], h["energy"]],
+                                      filepath=cfg.vtu_path(iter_num))
+        self._snap.submit({"rho": st.rho, "rho_projected": st.rho_projected,
+                           "energy": st.energy_mean}, write)
 
     def step_host(self, rho_host: torch.Tensor) -> float:
         """One iteration driven from host memory: copy ``rho_host`` (pinned,
@@ -396,10 +430,18 @@ class DensityMethod:
         return self.filter.design_reduce(op, x, y)
 
     def _finalize(self):
+        """common_density.py:944-964: histories.npz and the thresholded
+        design cubic_top.vtu (elements kept where rho > 0.5)."""
         if self._completed:
             return
         if self.cfg.export:
             self.recorder.export_histories(fname="histories.npz")
+            if self.cfg.export_vtu and self._state is not None:
+                from ..visualization import export_submesh
+                export_submesh(self.tsk, self._state.rho.cpu().numpy(), 0.5,
+                               f"{self.cfg.dst_path}/cubic_top.vtu")
+        if self._snap is not None:
+            self._snap.flush()
         self._completed = True
 
     def rho_update(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):

@@ -66,3 +66,25 @@ def test_batched_designs_reject_mixed_element_shapes(native_lib):
         return OC_Optimizer(cfg, tsk, device=_dev())
     with pytest.raises(ValueError):
         BatchedDesigns([_make((8, 4, 4, 0.3, 0.5), 2), stretched], device=_dev())
+
+
+def test_run_sharded_matches_solo_runs(native_lib):
+    """A rank's share of a sharded batch (partition by element count) gives
+    the same histories as running each design alone; without a process
+    group every rank returns its own share."""
+    from sktopt_gb300.core import partition_designs, run_sharded
+    specs = [(12, 6, 6, 0.3, 0.5), (16, 6, 6, 0.4, 0.1), (10, 5, 5, 0.3, 0.9),
+             (14, 7, 7, 0.35, 0.3), (12, 8, 6, 0.25, 0.6)]
+    makers = [_make(s, 2) for s in specs]
+    costs = [a * b * c for a, b, c, _, _ in specs]
+    solo = {}
+    for i, mk in enumerate(makers):
+        o = mk()
+        o.parameterize()
+        o.optimize_steps(2)
+        solo[i] = list(o.recorder.histories["compliance"])
+    for rank in range(2):
+        got = run_sharded(makers, costs, 2, rank=rank, world_size=2, n_workers=4)
+        assert sorted(got) == partition_designs(costs, 2)[rank]
+        for i, h in got.items():
+            assert h == solo[i], (i, h, solo[i])

@@ -91,3 +91,15 @@ def test_restart_from_checkpoint(native_lib, tmp_path):
     b.optimize()
     last = np.load(tmp_path / "data" / f"{n_iter:06d}-rho.npz")["rho_design_elements"]
     assert np.all(np.isfinite(last)) and last.shape == saved3.shape
+    # VTU of every saved iteration (rho_projected, energy) and the final
+    # thresholded design (common_density.py:1199-1204, 960-962)
+    from sktopt_gb300.core.visualization import read_vtu
+    vtus = sorted(os.listdir(tmp_path / "mesh_rho"))
+    assert vtus == [f"info_mesh-{i:08d}.vtu" for i in range(1, n_iter + 1)], vtus
+    v = read_vtu(tmp_path / "mesh_rho" / vtus[-1])
+    assert set(v["cell_data"]) == {"rho_projected", "energy"}
+    assert v["cell_data"]["rho_projected"].shape == (b.tsk.mesh.nelements,)
+    np.testing.assert_array_equal(v["cell_data"]["rho_projected"],
+                                  b._state.rho_projected.cpu().numpy())
+    top = read_vtu(tmp_path / "cubic_top.vtu")
+    assert 0 < top["connectivity"].shape[1] <= b.tsk.mesh.nelements
