@@ -193,6 +193,14 @@ int topt_filter_gauss_create(int64_t n_elem, const double* centers /* 3 x n */,
                              topt_filter** out);
 void topt_filter_destroy(topt_filter* f);
 int topt_filter_set_stream(topt_filter* f, void* cuda_stream);
+/* Declare the elements to be the cells of an nx x ny x nz grid (element
+ * e = ey + ny (ex + nx ez), the structured hex meshes).  When every row of W
+ * has the translation-invariant form W_kj = g(j - i) W_kk (checked against
+ * the whole matrix), the FP32 bracketing steps of topt_oc_bisect apply W as
+ * a stencil instead of the CSR; results and the FP64 steps are unchanged.
+ * n_offsets (topt_filter_stencil_size) is 0 when the check failed. */
+int topt_filter_set_grid(topt_filter* f, int32_t nx, int32_t ny, int32_t nz);
+int topt_filter_stencil_size(const topt_filter* f, int32_t* n_offsets);
 int topt_filter_sizes(const topt_filter* f, int64_t* n_design, int64_t* nnz);
 /* host export of W (design x design CSR) for checks */
 int topt_filter_export(const topt_filter* f, int32_t* rowptr, int32_t* colind,

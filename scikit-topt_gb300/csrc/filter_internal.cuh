@@ -36,4 +36,11 @@ struct topt_filter {
   topt::DevBuf cand, state, partials, counter, rho_e, rho_new;
   // FP32 bracketing of the bisection: W in FP32 and per-step inputs
   topt::DevBuf vals32, cand32, oc32;
+  // the same W as a stencil when the elements are the cells of an nx x ny x nz
+  // grid (e = ey + ny (ex + nx ez)) and every row has the translation-invariant
+  // form W_kj = g(j - i) W_kk: offsets with unnormalised weights g (int4:
+  // dx, dy, dz, float bits of g), W_kk per design row, the design mask
+  int grid[3] = {0, 0, 0};
+  int st_n = 0;                              // 0: no stencil
+  topt::DevBuf st_offs, st_invd, st_dmask;
 };

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <memory>
 #include <mutex>
 #include <new>
@@ -418,6 +419,139 @@ __global__ void k_oc_vol32(int64_t nd, const int32_t* __restrict__ rowptr,
   }
 }
 
+// k_oc_vol32 with W applied as a stencil on a structured grid: s_k = W_kk
+// sum_o g_o cand[e + o] over the design neighbours inside the grid, offsets
+// in the CSR column order (the candidate array, 4 bytes per element, stays in
+// L2 across the steps of a bisection).
+__global__ void k_oc_vol32s(int64_t nd, const int32_t* __restrict__ design, int nx, int ny,
+                            int nz, const int4* __restrict__ offs, int no,
+                            const float* __restrict__ invd, const uint8_t* __restrict__ dmask,
+                            const float* __restrict__ cand, const double* __restrict__ vol,
+                            double vol_sum, topt_oc_params prm, float tbe, float den,
+                            double err, OcState* st, double* partials, unsigned* counter) {
+  TOPT_KERNEL_COUNT();
+  if (st->done) return;
+  const float beta = (float)prm.beta, beta_eta = (float)prm.beta_eta;
+  float tacc = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int e = design[i];
+    const int ey = e % ny, ex = (e / ny) % nx, ez = e / (ny * nx);
+    float s = 0.0f;
+    for (int k = 0; k < no; ++k) {
+      const int4 o = __ldg(offs + k);
+      const int x = ex + o.x, y = ey + o.y, z = ez + o.z;
+      if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
+      const int j = y + ny * (x + nx * z);
+      if (dmask[j]) s += __int_as_float(o.w) * cand[j];
+    }
+    s *= invd[i];
+    const float hp = (tbe + tanhf((s - beta_eta) * beta)) / den;
+    tacc += hp * (float)vol[i];
+  }
+  double acc[1] = {(double)tacc};
+  __shared__ double sh[32];
+  __shared__ double total;
+  block_sum<double, 1>(acc, sh);
+  if (grid_finish<double, 1>(acc, partials, counter, &total)) {
+    if (threadIdx.x == 0) {
+      const double ve = total / vol_sum - prm.vol_frac;
+      const double a = fabs(ve);
+      if (!(a > err) || fabs(a - prm.vol_tol) <= err) {
+        st->need64 = 1;
+      } else {
+        st->need64 = 0;
+        st->vol_error = ve;
+        oc_decide(st, prm, ve);
+      }
+    }
+  }
+}
+
+// Derive the stencil form of W on an nx x ny x nz cell grid, or leave st_n
+// = 0 when some row does not have it (then the CSR kernel runs).  Offsets
+// are checked against every row: the same neighbour set (design cells of
+// the grid within the offset set) and W_kj = g_o W_kk to 1e-12.
+static int derive_stencil(topt_filter* f) {
+  f->st_n = 0;
+  const int nx = f->grid[0], ny = f->grid[1], nz = f->grid[2];
+  const int64_t n = f->n_elem, nd = f->n_design;
+  if (nx <= 0 || (int64_t)nx * ny * nz != n || nd == 0) return TOPT_OK;
+  std::vector<int32_t> design(nd);
+  TOPT_CUDA(cudaMemcpy(design.data(), f->design.p, sizeof(int32_t) * nd,
+                       cudaMemcpyDeviceToHost));
+  std::vector<uint8_t> dmask(n, 0);
+  for (int64_t k = 0; k < nd; ++k) dmask[design[k]] = 1;
+  auto coords = [&](int64_t e, int& x, int& y, int& z) {
+    y = (int)(e % ny);
+    x = (int)((e / ny) % nx);
+    z = (int)(e / ((int64_t)ny * nx));
+  };
+  // offsets and weights from the row with the most entries
+  int64_t best = 0;
+  for (int64_t k = 0; k < nd; ++k)
+    if (f->h_rowptr[k + 1] - f->h_rowptr[k] > f->h_rowptr[best + 1] - f->h_rowptr[best]) best = k;
+  struct Off { int dx, dy, dz; double g; };
+  std::vector<Off> offs;
+  {
+    int x0, y0, z0;
+    coords(design[best], x0, y0, z0);
+    double wkk = 0.0;
+    for (int32_t q = f->h_rowptr[best]; q < f->h_rowptr[best + 1]; ++q)
+      if (design[f->h_colind[q]] == design[best]) wkk = f->h_vals[q];
+    if (!(wkk > 0.0)) return TOPT_OK;
+    for (int32_t q = f->h_rowptr[best]; q < f->h_rowptr[best + 1]; ++q) {
+      int x, y, z;
+      coords(design[f->h_colind[q]], x, y, z);
+      offs.push_back({x - x0, y - y0, z - z0, f->h_vals[q] / wkk});
+    }
+  }
+  if (offs.empty() || offs.size() > 512) return TOPT_OK;
+  for (const Off& o : offs)
+    if (std::abs(o.dx) > 8 || std::abs(o.dy) > 8 || std::abs(o.dz) > 8) return TOPT_OK;
+  // CSR column order = ascending element index = ascending linear offset
+  std::sort(offs.begin(), offs.end(), [&](const Off& a, const Off& b) {
+    return (int64_t)a.dy + (int64_t)ny * (a.dx + (int64_t)nx * a.dz) <
+           (int64_t)b.dy + (int64_t)ny * (b.dx + (int64_t)nx * b.dz);
+  });
+  std::vector<float> invd(nd);
+  for (int64_t k = 0; k < nd; ++k) {
+    int x0, y0, z0;
+    const int64_t e = design[k];
+    coords(e, x0, y0, z0);
+    double wkk = 0.0;
+    for (int32_t q = f->h_rowptr[k]; q < f->h_rowptr[k + 1]; ++q)
+      if (design[f->h_colind[q]] == e) wkk = f->h_vals[q];
+    if (!(wkk > 0.0)) return TOPT_OK;
+    int32_t q = f->h_rowptr[k];
+    for (const Off& o : offs) {
+      const int x = x0 + o.dx, y = y0 + o.dy, z = z0 + o.dz;
+      if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
+      const int64_t j = y + (int64_t)ny * (x + (int64_t)nx * z);
+      if (!dmask[j]) continue;
+      if (q >= f->h_rowptr[k + 1] || design[f->h_colind[q]] != j) return TOPT_OK;
+      if (std::fabs(f->h_vals[q] - o.g * wkk) > 1e-12 * wkk) return TOPT_OK;
+      ++q;
+    }
+    if (q != f->h_rowptr[k + 1]) return TOPT_OK;
+    invd[k] = (float)wkk;
+  }
+  std::vector<int4> packed(offs.size());
+  for (size_t k = 0; k < offs.size(); ++k) {
+    const float g = (float)offs[k].g;
+    int gi;
+    std::memcpy(&gi, &g, sizeof(gi));
+    packed[k] = make_int4(offs[k].dx, offs[k].dy, offs[k].dz, gi);
+  }
+  int rc;
+  if ((rc = upload(f->st_offs, packed.data(), packed.size(), nullptr))) return rc;
+  if ((rc = upload(f->st_invd, invd.data(), invd.size(), nullptr))) return rc;
+  if ((rc = upload(f->st_dmask, dmask.data(), dmask.size(), nullptr))) return rc;
+  TOPT_CUDA(cudaDeviceSynchronize());
+  f->st_n = (int)offs.size();
+  return TOPT_OK;
+}
+
 // --------------------------------------------------------------------------
 // Reductions with host results.
 template <int OP>  // 0: max |x| (NaN-propagating), 1: dot
@@ -497,6 +631,20 @@ void topt_filter_destroy(topt_filter* f) {
   if (!f) return;
   cudaDeviceSynchronize();
   delete f;
+}
+
+int topt_filter_set_grid(topt_filter* f, int32_t nx, int32_t ny, int32_t nz) {
+  if (!f || nx < 0 || ny < 0 || nz < 0) return fail(TOPT_BAD_INPUT, "filter_set_grid: bad argument");
+  f->grid[0] = nx;
+  f->grid[1] = ny;
+  f->grid[2] = nz;
+  return derive_stencil(f);
+}
+
+int topt_filter_stencil_size(const topt_filter* f, int32_t* n_offsets) {
+  if (!f || !n_offsets) return fail(TOPT_BAD_INPUT, "filter_stencil_size: null argument");
+  *n_offsets = f->st_n;
+  return TOPT_OK;
 }
 
 int topt_filter_set_stream(topt_filter* f, void* s) {
@@ -616,10 +764,18 @@ int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rh
     for (int k = 0; k < max_steps; ++k) {
       k_oc_cand32<<<g, kFB, 0, f->stream>>>(nd, design, f->oc32.as<Oc32>(), st, *prm,
                                             f->cand32.as<float>());
-      k_oc_vol32<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(), f->colfull.as<int32_t>(),
-                                           f->vals32.as<float>(), f->cand32.as<float>(), vol,
-                                           vol_sum, *prm, (float)tbe, (float)den, err, st,
-                                           f->partials.as<double>(), f->counter.as<unsigned>());
+      if (f->st_n > 0)
+        k_oc_vol32s<<<g, kFB, 0, f->stream>>>(
+            nd, f->design.as<int32_t>(), f->grid[0], f->grid[1], f->grid[2],
+            f->st_offs.as<int4>(), f->st_n, f->st_invd.as<float>(), f->st_dmask.as<uint8_t>(),
+            f->cand32.as<float>(), vol, vol_sum, *prm, (float)tbe, (float)den, err, st,
+            f->partials.as<double>(), f->counter.as<unsigned>());
+      else
+        k_oc_vol32<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(),
+                                             f->colfull.as<int32_t>(), f->vals32.as<float>(),
+                                             f->cand32.as<float>(), vol, vol_sum, *prm,
+                                             (float)tbe, (float)den, err, st,
+                                             f->partials.as<double>(), f->counter.as<unsigned>());
       fp64_step(1);
     }
     fp64_step(2);   // exact candidate and volume error at the final lmid

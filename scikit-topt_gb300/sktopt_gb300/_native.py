@@ -102,6 +102,8 @@ SIGNATURES = {
     "topt_filter_gauss_create": (C.c_int, [_I64, _P, _P, _D, C.POINTER(_P)]),
     "topt_filter_destroy": (None, [_P]),
     "topt_filter_set_stream": (C.c_int, [_P, _P]),
+    "topt_filter_set_grid": (C.c_int, [_P, _I32, _I32, _I32]),
+    "topt_filter_stencil_size": (C.c_int, [_P, C.POINTER(_I32)]),
     "topt_filter_sizes": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64)]),
     "topt_filter_export": (C.c_int, [_P, _P, _P, _P]),
     "topt_filter_forward": (C.c_int, [_P, _P, _P]),

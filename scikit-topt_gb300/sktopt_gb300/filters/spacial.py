@@ -49,6 +49,10 @@ class SpacialFilter(DesignOps, BaseFilter):
                 self._mask.ctypes.data_as(C.c_void_p), float(radius), C.byref(h)))
         self.h = h
         self.radius = radius
+        # structured hex grid: the FP32 bisection steps may use W as a stencil
+        m = self.mesh
+        if getattr(m, "kind", None) == "hex" and getattr(m, "has_grid", False):
+            N.check(self.lib.topt_filter_set_grid(self.h, *[int(v) for v in m.shape]))
         nd, nnz = C.c_int64(), C.c_int64()
         N.check(self.lib.topt_filter_sizes(self.h, C.byref(nd), C.byref(nnz)))
         self.n_design, self.nnz = nd.value, nnz.value
@@ -63,6 +67,13 @@ class SpacialFilter(DesignOps, BaseFilter):
             self.close()
         except Exception:
             pass
+
+    @property
+    def stencil_size(self) -> int:
+        """Offsets of the stencil form of W (0: the FP32 steps use the CSR)."""
+        n = C.c_int32()
+        N.check(self.lib.topt_filter_stencil_size(self.h, C.byref(n)))
+        return n.value
 
     def update_radius(self, radius, **_):
         if radius != self.radius:

@@ -98,8 +98,9 @@ def test_oc_loop_matches_oracle(native_lib):
 
 
 def test_oc_fp32_bracketed_bisection_equals_fp64(native_lib):
-    """FP32-bracketed bisection takes the FP64 bisection's path: identical
-    lmid, volume error, step count and density at every iteration."""
+    """FP32-bracketed bisection (its FP32 steps on the stencil form of W)
+    takes the FP64 bisection's path: identical lmid, volume error, step count
+    and density at every iteration."""
     import dataclasses
     from sktopt_gb300.core import OC_Optimizer
     from sktopt_gb300.mesh import toy_problem
@@ -108,6 +109,8 @@ def test_oc_fp32_bracketed_bisection_equals_fp64(native_lib):
         cfg = dataclasses.replace(_oc_cfg(6), bisection_fp32_bracket=bracket)
         opt = OC_Optimizer(cfg, toy_problem.cantilever(24, 12, 12), device=_dev())
         opt.parameterize()
+        # the FP32 steps apply W as a 19-point stencil on this grid (r = 1.5)
+        assert opt.filter.stencil_size == 19
         steps, rhos = [], []
         for _ in range(6):
             opt.optimize_steps(1)
