@@ -87,6 +87,10 @@ struct topt_fem {
   bool mixed = false, has_grid = false;
   int mg_levels = 1, mg_coarse_max = 192;
   cudaStream_t stream = nullptr;
+  // side stream of the coarsest dense inverse (overlapped with the
+  // Chebyshev bounds of the other levels), created on first use
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int sm = 152;
   std::vector<topt::LevelStruct> ls;   // level 0 = fine mesh
   topt::DevBuf mask;                   // level-0 Dirichlet flags (uint8 per DOF)
@@ -722,25 +726,26 @@ static int estimate_lmax(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, doub
   return TOPT_OK;
 }
 
+// Dense inverse of the coarsest level, queued on stream s (no wait).
 template <typename T>
-static int build_dense(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, DevBuf& scratch) {
+static int build_dense(topt_fem* h, const LevelStruct& L, LevelNum<T>& N, DevBuf& scratch,
+                       cudaStream_t s) {
   const int n = L.ndense;
   int rc;
   if (scratch.bytes < sizeof(double) * (size_t)n * n &&
       (rc = scratch.alloc(sizeof(double) * (size_t)n * n)))
     return rc;
-  TOPT_CUDA(cudaMemsetAsync(scratch.p, 0, sizeof(double) * (size_t)n * n, h->stream));
+  TOPT_CUDA(cudaMemsetAsync(scratch.p, 0, sizeof(double) * (size_t)n * n, s));
   if (h->bs == 3)
-    k_sell_to_dense<T, 3><<<gridsize(h, L.npos), kBlock, 0, h->stream>>>(
+    k_sell_to_dense<T, 3><<<gridsize(h, L.npos), kBlock, 0, s>>>(
         L.npos, L.sell, N.vals.template as<T>(), n, scratch.as<double>());
   else
-    k_sell_to_dense<T, 1><<<gridsize(h, L.npos), kBlock, 0, h->stream>>>(
+    k_sell_to_dense<T, 1><<<gridsize(h, L.npos), kBlock, 0, s>>>(
         L.npos, L.sell, N.vals.template as<T>(), n, scratch.as<double>());
-  k_gauss_jordan_inverse<<<1, 1024, 0, h->stream>>>(n, scratch.as<double>());
-  k_dense_copy<T><<<gridsize(h, (int64_t)n * n), kBlock, 0, h->stream>>>(
+  k_gauss_jordan_inverse<<<1, 1024, 0, s>>>(n, scratch.as<double>());
+  k_dense_copy<T><<<gridsize(h, (int64_t)n * n), kBlock, 0, s>>>(
       (int64_t)n * n, scratch.as<double>(), N.dense_inv.template as<T>());
   TOPT_CHECK_LAUNCH("dense coarse");
-  TOPT_CUDA(cudaStreamSynchronize(h->stream));
   return TOPT_OK;
 }
 
@@ -785,6 +790,8 @@ static int refresh(topt_fem* h, Hier<T>& H) {
       return rc;
   }
   DevBuf& scratch = H.dense_scratch;
+  // every level's operator (each from the finer one) ...
+  int dense_li = -1;
   for (int li = 0; li < nlev; ++li) {
     LevelStruct& L = h->ls[li];
     LevelNum<T>& N = H.lv[li];
@@ -796,14 +803,31 @@ static int refresh(topt_fem* h, Hier<T>& H) {
       if ((rc = block_inv<T>(h, L, N.vals.template as<T>(), N.dinv.template as<T>(), true)))
         return rc;
     }
-    if (L.dense) {
-      if ((rc = build_dense<T>(h, L, N, scratch))) return rc;
-    } else if (nlev > 1) {
-      if ((rc = estimate_lmax<T>(h, L, N, &N.lmax))) return rc;
+    if (L.dense) dense_li = li;
+  }
+  // ... then the coarsest dense inverse (one CTA) on the side stream while
+  // the power iterations of the other levels run on the handle's stream
+  if (dense_li >= 0) {
+    if (!h->aux) {
+      TOPT_CUDA(cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking));
+      TOPT_CUDA(cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming));
+      TOPT_CUDA(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+    }
+    TOPT_CUDA(cudaEventRecord(h->ev_fork, h->stream));
+    TOPT_CUDA(cudaStreamWaitEvent(h->aux, h->ev_fork, 0));
+    if ((rc = build_dense<T>(h, h->ls[dense_li], H.lv[dense_li], scratch, h->aux))) return rc;
+    TOPT_CUDA(cudaEventRecord(h->ev_join, h->aux));
+  }
+  for (int li = 0; li < nlev; ++li) {
+    if (li == dense_li) continue;
+    LevelNum<T>& N = H.lv[li];
+    if (nlev > 1) {
+      if ((rc = estimate_lmax<T>(h, h->ls[li], N, &N.lmax))) return rc;
     } else {
       N.lmax = 0.0;
     }
   }
+  if (dense_li >= 0) TOPT_CUDA(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
   return TOPT_OK;
 }
 
@@ -1502,6 +1526,9 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
 void topt_fem_destroy(topt_fem* h) {
   if (!h) return;
   cudaDeviceSynchronize();
+  if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  if (h->aux) cudaStreamDestroy(h->aux);
   delete h;
 }
 
