@@ -42,5 +42,7 @@ struct topt_filter {
   // dx, dy, dz, float bits of g), W_kk per design row, the design mask
   int grid[3] = {0, 0, 0};
   int st_n = 0;                              // 0: no stencil
-  topt::DevBuf st_offs, st_invd, st_dmask;
+  topt::DevBuf st_invd;                      // W_kk per design row (float)
+  topt::DevBuf st_lin, st_g;                 // linear offset and weight per offset
+  topt::DevBuf st_nb;                        // per design row: bit o = neighbour o present
 };

@@ -420,30 +420,37 @@ __global__ void k_oc_vol32(int64_t nd, const int32_t* __restrict__ rowptr,
 }
 
 // k_oc_vol32 with W applied as a stencil on a structured grid: s_k = W_kk
-// sum_o g_o cand[e + o] over the design neighbours inside the grid, offsets
-// in the CSR column order (the candidate array, 4 bytes per element, stays in
-// L2 across the steps of a bisection).
-__global__ void k_oc_vol32s(int64_t nd, const int32_t* __restrict__ design, int nx, int ny,
-                            int nz, const int4* __restrict__ offs, int no,
-                            const float* __restrict__ invd, const uint8_t* __restrict__ dmask,
-                            const float* __restrict__ cand, const double* __restrict__ vol,
-                            double vol_sum, topt_oc_params prm, float tbe, float den,
-                            double err, OcState* st, double* partials, unsigned* counter) {
+// sum_o g_o cand[e + lin_o] over the offsets whose bit is set in the row's
+// neighbour mask (inside the grid and a design element), in the CSR column
+// order.  The candidate array (4 bytes per element) stays in L2 across the
+// steps of a bisection; the offsets sit in shared memory.
+__global__ void k_oc_vol32s(int64_t nd, const int32_t* __restrict__ design,
+                            const int32_t* __restrict__ lin, const float* __restrict__ gw,
+                            int no, const unsigned long long* __restrict__ nb,
+                            const float* __restrict__ invd, const float* __restrict__ cand,
+                            const double* __restrict__ vol, double vol_sum, topt_oc_params prm,
+                            float tbe, float den, double err, OcState* st, double* partials,
+                            unsigned* counter) {
   TOPT_KERNEL_COUNT();
   if (st->done) return;
+  __shared__ int s_lin[64];
+  __shared__ float s_g[64];
+  for (int k = threadIdx.x; k < no; k += blockDim.x) {
+    s_lin[k] = lin[k];
+    s_g[k] = gw[k];
+  }
+  __syncthreads();
   const float beta = (float)prm.beta, beta_eta = (float)prm.beta_eta;
   float tacc = 0.0f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nd;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const int e = design[i];
-    const int ey = e % ny, ex = (e / ny) % nx, ez = e / (ny * nx);
+    const int64_t e = design[i];
+    unsigned long long m = nb[i];
     float s = 0.0f;
-    for (int k = 0; k < no; ++k) {
-      const int4 o = __ldg(offs + k);
-      const int x = ex + o.x, y = ey + o.y, z = ez + o.z;
-      if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
-      const int j = y + ny * (x + nx * z);
-      if (dmask[j]) s += __int_as_float(o.w) * cand[j];
+    while (m) {
+      const int k = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      s += s_g[k] * cand[e + s_lin[k]];
     }
     s *= invd[i];
     const float hp = (tbe + tanhf((s - beta_eta) * beta)) / den;
@@ -506,7 +513,7 @@ static int derive_stencil(topt_filter* f) {
       offs.push_back({x - x0, y - y0, z - z0, f->h_vals[q] / wkk});
     }
   }
-  if (offs.empty() || offs.size() > 512) return TOPT_OK;
+  if (offs.empty() || offs.size() > 64) return TOPT_OK;
   for (const Off& o : offs)
     if (std::abs(o.dx) > 8 || std::abs(o.dy) > 8 || std::abs(o.dz) > 8) return TOPT_OK;
   // CSR column order = ascending element index = ascending linear offset
@@ -515,6 +522,7 @@ static int derive_stencil(topt_filter* f) {
            (int64_t)b.dy + (int64_t)ny * (b.dx + (int64_t)nx * b.dz);
   });
   std::vector<float> invd(nd);
+  std::vector<unsigned long long> nbm(nd, 0ull);
   for (int64_t k = 0; k < nd; ++k) {
     int x0, y0, z0;
     const int64_t e = design[k];
@@ -524,29 +532,31 @@ static int derive_stencil(topt_filter* f) {
       if (design[f->h_colind[q]] == e) wkk = f->h_vals[q];
     if (!(wkk > 0.0)) return TOPT_OK;
     int32_t q = f->h_rowptr[k];
-    for (const Off& o : offs) {
+    for (size_t oi = 0; oi < offs.size(); ++oi) {
+      const Off& o = offs[oi];
       const int x = x0 + o.dx, y = y0 + o.dy, z = z0 + o.dz;
       if (x < 0 || y < 0 || z < 0 || x >= nx || y >= ny || z >= nz) continue;
       const int64_t j = y + (int64_t)ny * (x + (int64_t)nx * z);
       if (!dmask[j]) continue;
       if (q >= f->h_rowptr[k + 1] || design[f->h_colind[q]] != j) return TOPT_OK;
       if (std::fabs(f->h_vals[q] - o.g * wkk) > 1e-12 * wkk) return TOPT_OK;
+      nbm[k] |= 1ull << oi;
       ++q;
     }
     if (q != f->h_rowptr[k + 1]) return TOPT_OK;
     invd[k] = (float)wkk;
   }
-  std::vector<int4> packed(offs.size());
+  std::vector<int32_t> lin(offs.size());
+  std::vector<float> gw(offs.size());
   for (size_t k = 0; k < offs.size(); ++k) {
-    const float g = (float)offs[k].g;
-    int gi;
-    std::memcpy(&gi, &g, sizeof(gi));
-    packed[k] = make_int4(offs[k].dx, offs[k].dy, offs[k].dz, gi);
+    lin[k] = (int32_t)(offs[k].dy + (int64_t)ny * (offs[k].dx + (int64_t)nx * offs[k].dz));
+    gw[k] = (float)offs[k].g;
   }
   int rc;
-  if ((rc = upload(f->st_offs, packed.data(), packed.size(), nullptr))) return rc;
+  if ((rc = upload(f->st_lin, lin.data(), lin.size(), nullptr))) return rc;
+  if ((rc = upload(f->st_g, gw.data(), gw.size(), nullptr))) return rc;
   if ((rc = upload(f->st_invd, invd.data(), invd.size(), nullptr))) return rc;
-  if ((rc = upload(f->st_dmask, dmask.data(), dmask.size(), nullptr))) return rc;
+  if ((rc = upload(f->st_nb, nbm.data(), nbm.size(), nullptr))) return rc;
   TOPT_CUDA(cudaDeviceSynchronize());
   f->st_n = (int)offs.size();
   return TOPT_OK;
@@ -766,10 +776,10 @@ int topt_oc_bisect(topt_filter* f, const double* dc, double dc_scale, double* rh
                                             f->cand32.as<float>());
       if (f->st_n > 0)
         k_oc_vol32s<<<g, kFB, 0, f->stream>>>(
-            nd, f->design.as<int32_t>(), f->grid[0], f->grid[1], f->grid[2],
-            f->st_offs.as<int4>(), f->st_n, f->st_invd.as<float>(), f->st_dmask.as<uint8_t>(),
-            f->cand32.as<float>(), vol, vol_sum, *prm, (float)tbe, (float)den, err, st,
-            f->partials.as<double>(), f->counter.as<unsigned>());
+            nd, f->design.as<int32_t>(), f->st_lin.as<int32_t>(), f->st_g.as<float>(), f->st_n,
+            f->st_nb.as<unsigned long long>(), f->st_invd.as<float>(), f->cand32.as<float>(),
+            vol, vol_sum, *prm, (float)tbe, (float)den, err, st, f->partials.as<double>(),
+            f->counter.as<unsigned>());
       else
         k_oc_vol32<<<g, kFB, 0, f->stream>>>(nd, f->rowptr.as<int32_t>(),
                                              f->colfull.as<int32_t>(), f->vals32.as<float>(),
