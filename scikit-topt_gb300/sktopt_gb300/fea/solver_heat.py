@@ -348,12 +348,12 @@ class FEM_SimpLinearHeatConduction:
         U.view(-1, L).copy_(X[:, :L])
         T = X[:, :L].contiguous()
         if obj == "compliance":
-            if self.has_robin or any(v != 0.0 for v in self.values):
-                KT = self.engine.spmv(T, full=True)
-            else:
-                KT = self.engine.spmv(T)
-            J = np.array([self._dot(T[:, i].contiguous(), KT[:, i].contiguous())
-                          for i in range(L)])
+            full = self.has_robin or any(v != 0.0 for v in self.values)
+            J = np.zeros(L)
+            for i in range(L):
+                t = T[:, i:i + 1].contiguous()
+                kt = self.engine.spmv(t, full=full)
+                J[i] = self._dot(t.view(-1), kt.view(-1))
             self.lam = None        # -2 T (solver_heat.py:789), formed on demand
         elif obj == "averaged_temp":
             J = np.array([self._dot(T[:, i].contiguous(), self._ones) for i in range(L)])
@@ -363,8 +363,10 @@ class FEM_SimpLinearHeatConduction:
                 self.lam = torch.zeros_like(T)
                 J = np.zeros(L)
             else:
-                _, num = self._ops.exchange(self._rho_n, T, self.h, self.t_env)
-                J = np.asarray(num) / den
+                num = np.concatenate([
+                    self._ops.exchange(self._rho_n, T[:, c:c + 4].contiguous(), self.h,
+                                       self.t_env)[1] for c in range(0, L, 4)])
+                J = num / den
                 lam = X[:, L:2 * L].clone()
                 w = self.task.avg_temp_weight
                 if w != 0.0:

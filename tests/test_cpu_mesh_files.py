@@ -146,10 +146,10 @@ def test_elastic_from_mesh_tags_matches_node_setup(tmp_path):
     R = osurf.surface_forces(om, [right, top], ["u^3", "u^2"], [-1.0, 0.25])
     for a, b in zip(t.neumann_linear, R):
         np.testing.assert_allclose(a, b, rtol=1e-13, atol=1e-15)
-    loaded = np.unique(np.concatenate([m.t[:, e] for e in range(m.nelements)
-                                       if np.any(np.isin(m.t[:, e],
-                                                         np.nonzero(np.abs(R[0]) + np.abs(R[1]))[0] // 3))]))
-    assert len(t.design_elements) < m.nelements and loaded.size > 0
+    # elements touching a loaded node leave the design set (task_common.py:208-227)
+    loaded_nodes = np.unique(np.nonzero(np.abs(R[0]) + np.abs(R[1]))[0] // 3)
+    touching = np.nonzero(np.isin(m.t, loaded_nodes).any(axis=0))[0]
+    assert touching.size > 0 and not np.isin(touching, t.design_elements).any()
 
 
 def test_heat_from_mesh_tags_matches_plate(tmp_path):
@@ -169,3 +169,48 @@ def test_heat_from_mesh_tags_matches_plate(tmp_path):
     for a, c in zip(t.robin_groups, ref.robin_groups):
         key = lambda x: np.lexsort(x.T[::-1])                 # noqa: E731
         assert np.array_equal(a[key(a)], c[key(c)])
+
+
+def test_msh_rejects_unsupported_input(tmp_path):
+    from sktopt_gb300.mesh import read_msh
+    (tmp_path / "bin.msh").write_text("$MeshFormat\n4.1 1 8\n$EndMeshFormat\n")
+    with pytest.raises(ValueError, match="binary"):
+        read_msh(tmp_path / "bin.msh")
+    (tmp_path / "none.msh").write_text("hello\n")
+    with pytest.raises(ValueError, match="not a gmsh"):
+        read_msh(tmp_path / "none.msh")
+    # a hexahedron and a tetrahedron in one file
+    mixed = """$MeshFormat
+2.2 0 8
+$EndMeshFormat
+$Nodes
+9
+1 0 0 0
+2 1 0 0
+3 1 1 0
+4 0 1 0
+5 0 0 1
+6 1 0 1
+7 1 1 1
+8 0 1 1
+9 2 0 0
+$EndNodes
+$Elements
+2
+1 5 2 0 0 1 2 3 4 5 6 7 8
+2 4 2 0 0 2 9 3 6
+$EndElements
+"""
+    (tmp_path / "mixed.msh").write_text(mixed)
+    with pytest.raises(ValueError, match="hexahedra or tetrahedra"):
+        read_msh(tmp_path / "mixed.msh")
+
+
+def test_traction_direction_and_length_checks():
+    from sktopt_gb300.mesh import assemble_surface_forces, boundary_facets, create_box_hex
+    m = create_box_hex(2, 2, 2)
+    f = boundary_facets(m)[:3]
+    with pytest.raises(ValueError):
+        assemble_surface_forces(m, [f, f], ["u^1"], [1.0, 2.0])
+    with pytest.raises(ValueError):
+        assemble_surface_forces(m, f, "x", 1.0)

@@ -110,6 +110,26 @@ def test_heat_robin_two_dirichlet_values(native_lib):
 
 
 @pytest.mark.parametrize("objective", ["compliance", "heat_exchange"])
+def test_heat_robin_five_dirichlet_values(native_lib, objective):
+    """Five load cases: the block solves, the compliance products and the
+    heat-exchange integrals run in chunks of at most four columns."""
+    from sktopt_gb300.mesh import toy_problem
+    vals = [600.0, 550.0, 500.0, 450.0, 400.0]
+    tsk = toy_problem.heat_plate(12, 12, 3, objective=objective, dirichlet_values=vals)
+    m, pb, *_ = problems.heat_plate(12, 12, 3, objective=objective, dirichlet_values=vals)
+    rho = np.random.default_rng(15).uniform(0.1, 1.0, m.nelements)
+    J_ref, T_ref = pb.objectives(rho, 3.0, 1e-2)
+    fem = _fem(tsk, "fp64")
+    u = np.zeros((tsk.n_dof, len(vals)))
+    J = fem.objectives_multi_load(rho, 3.0, u)
+    K, _, _ = pb.operator(rho, 3.0, 1e-2)
+    floor = max(4 * np.finfo(float).eps * (np.abs(T_ref[:, i]) @ (abs(K) @ np.abs(T_ref[:, i])))
+                for i in range(len(vals)))
+    np.testing.assert_allclose(J, J_ref, rtol=1e-9, atol=floor)
+    np.testing.assert_allclose(u, T_ref, rtol=0, atol=1e-8 * np.abs(T_ref).max())
+
+
+@pytest.mark.parametrize("objective", ["compliance", "heat_exchange"])
 def test_heat_robin_oc_loop_matches_oracle(native_lib, objective):
     """OC loop on the plate (compliance: the reference flow test's task) against
     the oracle loop: per-iteration objective 1e-8 (the compliance cancels,
