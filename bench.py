@@ -50,7 +50,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
-    ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd", "heat_robin"],
+    ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd", "heat_robin",
+                                        "multiload"],
                     default=None,
                     help="profiling target instead of the benchmark")
     return ap.parse_args()
@@ -668,6 +669,53 @@ def probe_heat_robin(size=(200, 200, 25), small=(40, 40, 5), iters=5, warmup=3):
     print(json.dumps(out))
 
 
+def probe_multiload(size=(160, 80, 40), iters=2):
+    """The multi-load unstructured configuration at full size: a 2 x 1 x 1
+    box of size[0] x size[1] x size[2] cubes split into 6 P1 tetrahedra each
+    (3,072,000 tets), interior nodes jittered by U(-0.2 h, 0.2 h) (seed 0),
+    bottom face clamped, 4 point-load cases solved as one 4-column block
+    right-hand side; log-space MOC, volume fraction 0.25, Helmholtz filter
+    r = 0.04.  One untimed iteration, then `iters` timed ones, FP64 and
+    mixed; the per-iteration compliance of the mixed path against FP64."""
+    import torch
+    from sktopt_gb300 import tools
+    from sktopt_gb300.core import LogMOC_Config, LogMOC_Optimizer
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", 0)
+    out = {"probe": "multiload", "size": list(size)}
+    hist = {}
+    for prec in ("fp64", "mixed"):
+        t0 = time.perf_counter()
+        tsk = toy_problem.multi_load_tet(*size, 2.0, 1.0, 1.0, jitter=0.2, seed=0)
+        cfg = LogMOC_Config(max_iters=iters + 1, filter_type="helmholtz",
+                            filter_radius=tools.SchedulerConfig.constant(target_value=0.04),
+                            p=tools.SchedulerConfig.constant(target_value=3.0),
+                            vol_frac=tools.SchedulerConfig.constant(target_value=0.25),
+                            move_limit=tools.SchedulerConfig.constant(target_value=0.2),
+                            E_min_coeff=1e-9, solver_option="cg_pyamg", precision=prec)
+        opt = LogMOC_Optimizer(cfg, tsk, device=dev)
+        opt.parameterize()
+        opt.optimize_steps(1)
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        opt.optimize_steps(iters)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / iters
+        st = opt.fem.last_stats
+        hist[prec] = list(opt.recorder.histories["compliance"])
+        out[prec] = {"ms_per_iter": round(dt * 1e3, 1), "setup_and_first_iter_s": round(setup, 1),
+                     "n_elem": tsk.mesh.nelements, "n_dof": tsk.n_dof, "loads": tsk.n_tasks,
+                     "solve_iters": st.iters, "relres": st.relres}
+        del opt
+        torch.cuda.empty_cache()
+    out["compliance_rel_err_per_iter"] = [abs(a - b) / abs(b)
+                                          for a, b in zip(hist["mixed"], hist["fp64"])]
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["ms_per_iter"] /
+                                         out["mixed"]["ms_per_iter"], 2)
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.probe == "spmv":
@@ -684,6 +732,9 @@ def main():
         return
     if args.probe == "heat_robin":
         probe_heat_robin()
+        return
+    if args.probe == "multiload":
+        probe_multiload()
         return
     if args.impl == "reference":
         run_reference(args)

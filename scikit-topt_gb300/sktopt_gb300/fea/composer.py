@@ -109,8 +109,10 @@ def tet_matrices(coords, nu):
     G = np.transpose(Ainv[:, 1:, :], (0, 2, 1))            # (e, 4, 3)
     V = np.abs(np.linalg.det(A)) / 6.0
     B = _strain_operator(G)                                # (e, 6, 12)
-    Ke = V[:, None, None] * np.einsum("eik,ij,ejl->ekl", B, _elastic_D(nu), B)
-    Kh = V[:, None, None] * np.einsum("ead,ebd->eab", G, G)
+    # B^T D B and G G^T as batched matrix products (BLAS), not einsum loops
+    Ke = V[:, None, None] * np.matmul(np.transpose(B, (0, 2, 1)),
+                                      np.matmul(_elastic_D(nu)[None], B))
+    Kh = V[:, None, None] * np.matmul(G, np.transpose(G, (0, 2, 1)))
     M = (V / 20.0)[:, None, None] * (np.ones((4, 4)) + np.eye(4))[None]
     return Ke, Kh, M
 
