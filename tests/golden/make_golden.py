@@ -67,11 +67,54 @@ def oc_trajectory(nx=12, ny=6, nz=6, n_iter=5):
                 rho=np.array(rhos))
 
 
-def main():
-    np.savez_compressed(os.path.join(HERE, "cantilever_10x5x4_state.npz"), **cantilever_state())
-    np.savez_compressed(os.path.join(HERE, "cantilever_12x6x6_oc5.npz"), **oc_trajectory())
-    print("wrote fixtures to", HERE)
+def heat_plate_state(nx=12, ny=12, nz=3, seed=11):
+    """The heat task of the reference's flow test on an nx x ny x nz plate:
+    objectives, temperatures, adjoints, energies and sensitivities for the
+    three objectives (heat exchange with avg_temp_weight 0.5)."""
+    from oracle import heat_robin as hr
+    out = {"shape": np.array([nx, ny, nz])}
+    rho = None
+    for obj, w in (("compliance", 0.0), ("heat_exchange", 0.5), ("averaged_temp", 0.0)):
+        m, pb, *_ = problems.heat_plate(nx, ny, nz, objective=obj, avg_temp_weight=w)
+        if rho is None:
+            rho = np.random.default_rng(seed).uniform(0.1, 1.0, m.nelements)
+            out["rho"] = rho
+            out["rho_nodal"] = hr.nodal_average(m, rho, "reference")[0]
+        J, T = pb.objectives(rho, 3.0, 1e-2)
+        out[f"{obj}_J"] = J
+        out[f"{obj}_T"] = T
+        if pb.lam is not None:
+            out[f"{obj}_lam"] = pb.lam
+        out[f"{obj}_energy"] = pb.energy(rho, 3.0, 1e-2, T)
+        out[f"{obj}_dc"] = pb.custom_sensitivity(rho, 3.0, 1e-2, T)
+    return out
+
+
+def tet_tractions(seed=4):
+    """Boundary facets and two traction load cases on a jittered tet box."""
+    from oracle import surface as osurf
+    from oracle import mesh as omesh
+    m = omesh.create_box_tet(5, 3, 3, 2.0, 1.0, 1.0, jitter=0.25, seed=seed)
+    f1 = osurf.boundary_facets(m, problems.in_range((2.0, 2.0), (0, 9), (0, 9)))
+    f2 = osurf.boundary_facets(m, problems.in_range((0, 2.0), (1.0, 1.0), (0, 9)))
+    F = osurf.surface_forces(m, [f1, f2], ["u^3", "u^1"], [-2.0, 0.5])
+    return dict(p=m.p, t=m.t, facets1=f1, facets2=f2, F1=F[0], F2=F[1])
+
+
+FIXTURES = {
+    "cantilever_10x5x4_state.npz": cantilever_state,
+    "cantilever_12x6x6_oc5.npz": oc_trajectory,
+    "heat_plate_12x12x3.npz": heat_plate_state,
+    "tet_tractions.npz": tet_tractions,
+}
+
+
+def main(names=None):
+    """Write the fixtures named on the command line (default: all)."""
+    for name in (names or FIXTURES):
+        np.savez_compressed(os.path.join(HERE, name), **FIXTURES[name]())
+        print("wrote", name)
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -12,7 +12,10 @@
   and both reproduce a uniform density;
 * without Robin data and with T = 0 Dirichlet values the compliance
   objective equals the plain conduction problem's;
-* the plate task's Dirichlet nodes and Robin facets match the oracle's.
+* the plate task's Dirichlet nodes and Robin facets match the oracle's;
+* the oracle reproduces its committed golden fixtures (heat plate objectives,
+  adjoints, energies, sensitivities; tet traction loads, also against the
+  product's host-side traction assembly).
 """
 import numpy as np
 import pytest
@@ -143,3 +146,45 @@ def test_oracle_objectives_run(objective):
     assert np.abs(T[pb.D] - 600.0).max() == 0.0
     g = pb.custom_sensitivity(rho, 3.0, 1e-2, T)
     assert g.shape == (m.nelements, 1) and np.all(np.isfinite(g))
+
+
+# --- golden fixtures (tests/golden/make_golden.py) ----------------------------
+def test_heat_oracle_matches_golden():
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "heat_plate_12x12x3.npz"))
+    nx, ny, nz = (int(v) for v in g["shape"])
+    rho = g["rho"]
+    for obj, w in (("compliance", 0.0), ("heat_exchange", 0.5), ("averaged_temp", 0.0)):
+        m, pb, *_ = problems.heat_plate(nx, ny, nz, objective=obj, avg_temp_weight=w)
+        if obj == "compliance":
+            assert np.array_equal(hr.nodal_average(m, rho, "reference")[0], g["rho_nodal"])
+        J, T = pb.objectives(rho, 3.0, 1e-2)
+        np.testing.assert_allclose(J, g[f"{obj}_J"], rtol=1e-11)
+        np.testing.assert_allclose(T, g[f"{obj}_T"], rtol=0, atol=1e-10)
+        if f"{obj}_lam" in g:
+            assert np.linalg.norm(pb.lam - g[f"{obj}_lam"]) <= \
+                1e-10 * np.linalg.norm(g[f"{obj}_lam"])
+        for key, val in (("energy", pb.energy(rho, 3.0, 1e-2, T)),
+                         ("dc", pb.custom_sensitivity(rho, 3.0, 1e-2, T))):
+            ref = g[f"{obj}_{key}"]
+            assert np.linalg.norm(val - ref) <= 1e-9 * np.linalg.norm(ref), (obj, key)
+
+
+def test_tractions_match_golden():
+    import os
+    from oracle import mesh as omesh
+    from oracle import surface as osurf
+    from sktopt_gb300.mesh import GridMesh, assemble_surface_forces, boundary_facets
+    from sktopt_gb300.mesh import get_points_in_range as rng
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "tet_tractions.npz"))
+    m = GridMesh(g["p"], g["t"], "tet")
+    f1 = boundary_facets(m, rng((2.0, 2.0), (0, 9), (0, 9)))
+    f2 = boundary_facets(m, rng((0, 2.0), (1.0, 1.0), (0, 9)))
+    assert np.array_equal(f1, g["facets1"]) and np.array_equal(f2, g["facets2"])
+    F = assemble_surface_forces(m, [f1, f2], ["u^3", "u^1"], [-2.0, 0.5])
+    np.testing.assert_allclose(F[0], g["F1"], rtol=1e-13, atol=1e-15)
+    np.testing.assert_allclose(F[1], g["F2"], rtol=1e-13, atol=1e-15)
+    om = omesh.GridMesh(g["p"], g["t"], "tet", None, None, None)
+    R = osurf.surface_forces(om, [f1, f2], ["u^3", "u^1"], [-2.0, 0.5])
+    np.testing.assert_array_equal(R[0], g["F1"])
+    np.testing.assert_array_equal(R[1], g["F2"])
