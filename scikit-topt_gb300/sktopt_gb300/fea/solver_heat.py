@@ -192,7 +192,6 @@ class FEM_SimpLinearHeatConduction:
         self.solver_option = self.solver_config.solver
         self.q = q
         self.nodal_pairing = nodal_pairing
-        self.device = device or default_device()
         v = getattr(task, "dirichlet_values", 0.0)
         self.values = [float(x) for x in v] if isinstance(v, (list, tuple)) else [float(v)]
         self.h = getattr(task, "robin_coefficient", None)
@@ -204,6 +203,7 @@ class FEM_SimpLinearHeatConduction:
             raise ValueError("the density-dependent Robin terms take one scalar "
                              "robin_coefficient and robin_bc_value (get_robin_virtual)")
         self.has_robin = self.virtual or len(self.groups) > 0
+        self.device = device or default_device()
         self._engine = None
         self._ops = None
         self._F = None

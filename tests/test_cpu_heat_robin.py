@@ -188,3 +188,29 @@ def test_tractions_match_golden():
     R = osurf.surface_forces(om, [f1, f2], ["u^3", "u^1"], [-2.0, 0.5])
     np.testing.assert_array_equal(R[0], g["F1"])
     np.testing.assert_array_equal(R[1], g["F2"])
+
+
+def test_heat_plugin_argument_checks():
+    """Host-side validation of the heat plugin (no GPU work): unknown
+    objectives, per-group coefficients for the density-dependent Robin terms,
+    Robin facets on tetrahedra, the nodal pairing name."""
+    import dataclasses
+    from sktopt_gb300.fea.solver_heat import FEM_SimpLinearHeatConduction
+    from sktopt_gb300.mesh import LinearHeatConduction, create_box_tet, toy_problem
+    tsk = toy_problem.heat_plate(10, 10, 2)
+    with pytest.raises(ValueError):
+        FEM_SimpLinearHeatConduction(dataclasses.replace(tsk, objective="flux"), 1e-3)
+    with pytest.raises(ValueError):
+        FEM_SimpLinearHeatConduction(dataclasses.replace(tsk, robin_coefficient=[4e-5, 4e-5]),
+                                     1e-3)
+    with pytest.raises(ValueError):
+        FEM_SimpLinearHeatConduction(tsk, 1e-3, nodal_pairing="rows")
+    with pytest.raises(ValueError):
+        LinearHeatConduction.from_nodes(tsk.mesh, tsk.dirichlet_nodes, None,
+                                        np.arange(tsk.mesh.nelements), objective="flux")
+    m = create_box_tet(3, 2, 2, 1.0, 1.0, 1.0)
+    from sktopt_gb300.mesh import boundary_facets
+    f = boundary_facets(m)[:2]
+    with pytest.raises(NotImplementedError):
+        LinearHeatConduction.from_facets(m, f, 1.0, f, 1e-3, 300.0, True,
+                                         np.arange(m.nelements), 1.0)
