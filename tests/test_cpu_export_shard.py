@@ -105,3 +105,22 @@ def test_two_gloo_ranks_gather_design_results():
     for r, p in enumerate(parts):
         for i in p:
             assert got[i] == [float(i), float(r)]
+
+
+def test_partition_more_ranks_than_designs():
+    from sktopt_gb300.core import partition_designs
+    parts = partition_designs([3.0, 1.0, 2.0], 5)
+    assert sorted(i for p in parts for i in p) == [0, 1, 2]
+    assert sum(1 for p in parts if not p) == 2
+
+
+def test_vtu_tetrahedra_with_point_data(tmp_path):
+    from sktopt_gb300.core.visualization import read_vtu, write_vtu
+    from sktopt_gb300.mesh import create_box_tet
+    m = create_box_tet(2, 2, 1, 1.0, 1.0, 0.5, jitter=0.1, seed=3)
+    pd = np.arange(m.nnodes, dtype=float)
+    cd = np.linspace(-1, 1, m.nelements)
+    write_vtu(tmp_path / "t.vtu", m.p, m.t, "tet", cell_data={"c": cd}, point_data={"T": pd})
+    r = read_vtu(tmp_path / "t.vtu")
+    assert np.all(r["types"] == 10) and np.array_equal(r["connectivity"], m.t)
+    assert np.array_equal(r["point_data"]["T"], pd) and np.array_equal(r["cell_data"]["c"], cd)

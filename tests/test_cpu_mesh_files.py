@@ -214,3 +214,28 @@ def test_traction_direction_and_length_checks():
         assemble_surface_forces(m, [f, f], ["u^1"], [1.0, 2.0])
     with pytest.raises(ValueError):
         assemble_surface_forces(m, f, "x", 1.0)
+
+
+def test_msh41_cell_in_two_physical_groups(tmp_path):
+    """A volume entity carrying two physical tags: its cells appear once in the
+    mesh and in both subdomains."""
+    from sktopt_gb300.mesh import read_msh
+    text = _MSH41.replace('3\n2 1 "dirichlet"\n2 2 "neumann"\n3 3 "design"',
+                          '4\n2 1 "dirichlet"\n2 2 "neumann"\n3 3 "design"\n3 4 "solid"')
+    # volume entity 1: bounding box, 2 physical tags (3, 4), no bounding surfaces
+    text = text.replace("1 0 0 0 2 1 1 1 3 0\n$EndEntities", "1 0 0 0 2 1 1 2 3 4 0\n$EndEntities")
+    nid = lambda x, y, z: 1 + x + 3 * y + 6 * z          # noqa: E731
+    xyz = [(x, y, z) for z in range(2) for y in range(2) for x in range(3)]
+    gm = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    hexes = [" ".join(str(nid(x + o[0], o[1], o[2])) for o in gm) for x in (0, 1)]
+    text = text.format(
+        tags="\n".join(str(nid(*c)) for c in xyz),
+        xyz="\n".join(f"{c[0]}.0 {c[1]}.0 {c[2]}.0" for c in xyz),
+        q0=" ".join(str(nid(0, y, z)) for y, z in ((0, 0), (1, 0), (1, 1), (0, 1))),
+        q1=" ".join(str(nid(2, y, z)) for y, z in ((0, 0), (1, 0), (1, 1), (0, 1))),
+        h0=hexes[0], h1=hexes[1])
+    (tmp_path / "g.msh").write_text(text)
+    m = read_msh(tmp_path / "g.msh")
+    assert m.nelements == 2
+    assert np.array_equal(m.subdomains["design"], [0, 1])
+    assert np.array_equal(m.subdomains["solid"], [0, 1])
