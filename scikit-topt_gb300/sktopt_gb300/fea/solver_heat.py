@@ -202,7 +202,9 @@ class FEM_SimpLinearHeatConduction:
                              isinstance(self.t_env, (list, tuple))):
             raise ValueError("the density-dependent Robin terms take one scalar "
                              "robin_coefficient and robin_bc_value (get_robin_virtual)")
-        self.has_robin = self.virtual or len(self.groups) > 0
+        if self.groups and not self.virtual:
+            raise ValueError("Robin facets need robin_coefficient and robin_bc_value")
+        self.has_robin = self.virtual
         self.device = device or default_device()
         self._engine = None
         self._ops = None
@@ -252,7 +254,6 @@ class FEM_SimpLinearHeatConduction:
             self._extra = torch.empty(mesh.nelements * 64, dtype=torch.float64, device=dev)
             self._vload = torch.zeros(n, dtype=torch.float64, device=dev)
             self._rho_n = torch.empty(n, dtype=torch.float64, device=dev)
-            self._surface_only_ready = False
         self._F = torch.from_numpy(F).to(dev)
         self._ones = torch.ones(n, dtype=torch.float64, device=dev)
 
@@ -260,13 +261,9 @@ class FEM_SimpLinearHeatConduction:
     def build(self, rho: torch.Tensor, p: float):
         eng = self.engine
         if self.has_robin:
-            if self.virtual:
-                self._ops.nodal_average(rho, self._rho_n)
-                self._ops.robin(self._rho_n, self.h, self.t_env, p, self.q, True, self._extra,
-                                self._vload)
-            elif not self._surface_only_ready:
-                self._ops.robin(None, 0.0, 0.0, p, self.q, False, self._extra, None)
-                self._surface_only_ready = True
+            self._ops.nodal_average(rho, self._rho_n)
+            self._ops.robin(self._rho_n, self.h, self.t_env, p, self.q, True, self._extra,
+                            self._vload)
             eng.set_extra(self._extra.view(-1, 8, 8))
         eng.update(rho, self.k_max, self.k_min, p)
         self._p = float(p)

@@ -205,6 +205,8 @@ def test_heat_plugin_argument_checks():
                                      1e-3)
     with pytest.raises(ValueError):
         FEM_SimpLinearHeatConduction(tsk, 1e-3, nodal_pairing="rows")
+    with pytest.raises(ValueError, match="robin_coefficient"):
+        FEM_SimpLinearHeatConduction(dataclasses.replace(tsk, robin_coefficient=None), 1e-3)
     with pytest.raises(ValueError):
         LinearHeatConduction.from_nodes(tsk.mesh, tsk.dirichlet_nodes, None,
                                         np.arange(tsk.mesh.nelements), objective="flux")
