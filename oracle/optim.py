@@ -91,16 +91,22 @@ class OracleConfig:
     p: Sched = field(default_factory=lambda: Sched("Step", 1.0, 3.0, 3))
     vol_frac: Sched = field(default_factory=lambda: Sched("Constant", 0.8, 0.8))
     beta: Sched = field(default_factory=lambda: Sched("StepAccelerating", 1.0, 2.0, 3, 2.0))
-    move_limit: Sched = field(default_factory=lambda: Sched("SawtoothDecay", 0.3, 0.1, 3))
-    eta: Sched = field(default_factory=lambda: Sched("Constant", 0.5, 0.5))
+    # sawtooth_decay("move_limit", 0.3, 0.1, 3) binds 3 to iters_max, so the
+    # cycle count keeps its default of 6 (scheduler.py:659-683)
+    move_limit: Sched = field(default_factory=lambda: Sched("SawtoothDecay", 0.3, 0.1, 6))
+    # None: OC_Config's constant 0.5 (oc.py:98-108) for "oc", the base
+    # DensityMethodConfig's 0.6 (common_density.py:62-345) for "logmoc"
+    eta: Sched | None = None
     percentile: Sched = field(default_factory=lambda: Sched("None"))
     filter_radius: Sched = field(default_factory=lambda: Sched("Constant", 0.01, 0.01))
     neumann_scale: Sched = field(default_factory=lambda: Sched("ConstantOne", 1.0, 1.0))
     E_min_coeff: float = 1e-3
     rho_min: float = 1e-2
     rho_max: float = 1.0
-    lambda_lower: float = 1e-7
-    lambda_upper: float = 1e7
+    # None: DensityMethod_OC_Config's 1e-7 / 1e7 for "oc", LogMOC_Config's
+    # -1e7 / 1e7 for "logmoc" (logmoc.py:13-33)
+    lambda_lower: float | None = None
+    lambda_upper: float | None = None
     scaling_rate_min: float = 0.7
     scaling_rate_max: float = 1.3
     sensitivity_scale_floor: float = 1e-12
@@ -116,6 +122,15 @@ class OracleConfig:
     solver: str = "spsolve"
     interpolation: str = "SIMP"        # "SIMP" | "RAMP" (common_density.py:392-404)
     rtol: float = 1e-8
+
+    def __post_init__(self):
+        if self.eta is None:
+            v = 0.5 if self.method == "oc" else 0.6
+            self.eta = Sched("Constant", v, v)
+        if self.lambda_lower is None:
+            self.lambda_lower = 1e-7 if self.method == "oc" else -1e7
+        if self.lambda_upper is None:
+            self.lambda_upper = 1e7
 
 
 class OracleOptimizer:

@@ -366,7 +366,7 @@ class DensityMethod:
             st.dC_drho_full.copy_(tmp)
         st.compliance = compliance_avg
         T.mark("rho_update")
-        self.rho_update(iter_num, st, move_limit, eta, beta, percentile, vol_frac)
+        self.rho_update_device(iter_num, st, move_limit, eta, beta, percentile, vol_frac)
         T.mark("metrics")
         rcm = self.filter_design_reduce(1, st.rho, st.rho_prev)
         T.mark("end")
@@ -448,5 +448,74 @@ class DensityMethod:
             self._snap.flush()
         self._completed = True
 
-    def rho_update(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
+    def rho_update_device(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
+        """The update on the device-resident state (the loop's own call):
+        reads st.dC_drho_full, st.rho, st.rho_filtered, st.rho_projected and
+        updates st.rho and st.scaling_rate in place."""
+        raise NotImplementedError("")
+
+    def rho_update(self, iter_num, rho_design_eles, rho_projected, dC_drho_design_eles,
+                   u_dofs, strain_energy_mean, scaling_rate, move_limit, eta, beta,
+                   rho_clip_lower, rho_clip_upper, percentile, elements_volume_design,
+                   elements_volume_design_sum, vol_frac):
+        """The reference's update hook with its positional signature, as the
+        driver calls it (common_density.py:1112-1129; received at
+        oc.py:149-167 and logmoc.py:90-108), for callers that keep their own
+        loop.  Arguments are NumPy arrays (or tensors) in the reference's
+        layout; they are mutated in place as the reference mutates them:
+
+        * ``rho_design_eles``: the updated design densities;
+        * ``scaling_rate``: OC -- the clipped multiplicative factor of the last
+          bisection step; log-MOC -- the clipped scaled Lagrangian gradient;
+        * ``rho_clip_lower`` / ``rho_clip_upper``: the move-limit bounds (OC:
+          in density; log-MOC: in log-density, logmoc.py:47-60);
+        * ``dC_drho_design_eles`` (OC only): divided by the running scale.
+
+        As in the reference, the full density (non-design entries) comes from
+        this optimizer's state, and ``u_dofs`` / ``strain_energy_mean`` are
+        not used.  The filtered density the log-MOC volume chain needs is the
+        filter applied to that full density, which is what the driver's state
+        holds at this point of the iteration (common_density.py:1043-1045).
+        ``elements_volume_design`` must be the task's design-element volumes
+        (the only values the reference passes)."""
+        if not self._ensure_state_initialized():
+            raise RuntimeError("optimization already completed")
+        st = self._state
+        dev = self.device
+
+        def dev64(x):
+            return torch.as_tensor(np.asarray(x) if not isinstance(x, torch.Tensor) else x,
+                                   dtype=torch.float64).to(dev)
+
+        def put(dst, src):
+            if isinstance(dst, torch.Tensor):
+                dst.copy_(src)
+            else:
+                dst[...] = src.cpu().numpy()
+
+        ev = dev64(elements_volume_design)
+        if ev.numel() != self._vol_design.numel() or \
+                not torch.equal(ev, self._vol_design):
+            raise ValueError("elements_volume_design must be the volumes of the task's "
+                             "design elements")
+        if not np.isclose(float(elements_volume_design_sum), self._vol_design_sum,
+                          rtol=1e-14, atol=0.0):
+            raise ValueError("elements_volume_design_sum must be their sum")
+        rho_e = dev64(rho_design_eles)
+        st.rho[self.design] = rho_e
+        st.rho_projected.copy_(dev64(rho_projected))
+        self.filter.forward_device(st.rho, out=st.rho_filtered)
+        st.dC_drho_full.zero_()
+        st.dC_drho_full[self.design] = dev64(dC_drho_design_eles)
+        self.rho_update_device(iter_num, st, move_limit, eta, beta, percentile, vol_frac)
+        put(rho_design_eles, st.rho[self.design])
+        put(scaling_rate, st.scaling_rate)
+        lower, upper, dc_scale = self._clip_bounds(rho_e, move_limit)
+        put(rho_clip_lower, lower)
+        put(rho_clip_upper, upper)
+        if dc_scale is not None:
+            put(dC_drho_design_eles, st.dC_drho_full[self.design] / dc_scale)
+
+    def _clip_bounds(self, rho_e, move_limit):
+        """(lower, upper, dC scale or None) of the method's update."""
         raise NotImplementedError("")

@@ -77,7 +77,7 @@ class LogMOC_Optimizer(DensityMethod):
             self._buf["dVp"][self.design] = self._dV_drho_design
         return self._buf
 
-    def rho_update(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
+    def rho_update_device(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
         """logmoc.py:90-258."""
         cfg, flt = self.cfg, self.filter
         B = self._buffers()
@@ -146,3 +146,13 @@ class LogMOC_Optimizer(DensityMethod):
         rec.feed_data("vol_error", vol_error)
         rec.feed_data("volume_chain_scale", chain_scale)
         rec.feed_data("kkt_residual", self.kkt_residual)
+
+    def _clip_bounds(self, rho_e, move_limit):
+        """The log-space bounds of lagrangian_log_update (logmoc.py:47-60):
+        with r = clip(rho, rho_min, rho_max) and d = log(1 + move / r),
+        lower = log r - d and upper = lower + 2 d."""
+        cfg = self.cfg
+        lr = torch.log(torch.clamp(rho_e, cfg.rho_min, cfg.rho_max))
+        d = torch.log(move_limit / torch.exp(lr) + 1.0)
+        lower = lr - d
+        return lower, lower + 2.0 * d, None

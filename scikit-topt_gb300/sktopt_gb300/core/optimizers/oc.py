@@ -15,6 +15,7 @@ from dataclasses import dataclass, field
 from typing import Literal
 
 import numpy as np
+import torch
 
 from ... import _native as N
 from ... import tools
@@ -41,7 +42,7 @@ class OC_Optimizer(DensityMethod):
         self.running_scale = 0.0
         self.last_bisection_steps = 0
 
-    def rho_update(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
+    def rho_update_device(self, iter_num, st, move_limit, eta, beta, percentile, vol_frac):
         cfg = self.cfg
         flt = self.filter
         if isinstance(percentile, float):
@@ -72,3 +73,11 @@ class OC_Optimizer(DensityMethod):
         self.recorder.feed_data("lmid", lmid)
         self.recorder.feed_data("vol_error", verr)
         self.recorder.feed_data("kkt_residual", self.kkt_residual)
+
+    def _clip_bounds(self, rho_e, move_limit):
+        """oc.py:59-60 (bounds around the densities before the update) and the
+        normalisation dC /= running_scale of oc.py:193."""
+        cfg = self.cfg
+        lower = torch.clamp(rho_e - move_limit, min=cfg.rho_min)
+        upper = torch.clamp(rho_e + move_limit, max=cfg.rho_max)
+        return lower, upper, self.running_scale
