@@ -204,40 +204,94 @@ def _event_time(fn, n=20):
 
 
 def roofline(opt, peak_gbs):
-    """Roofline of the kernel with the largest share of the mixed OC iteration:
-    the FP32 matrix-free operator k_mf_tile (four launches per V-cycle plus
-    the search-direction product), timed through the FP32 operator call with
-    CUDA events on the launching stream.  Algorithmic bytes per launch: x and
-    y (2 * 12 B per node), the fixed-DOF flags (4 B per node) and the cell
-    coefficients (4 B per cell).  The kernel is bound by FP32 FMA issue (576
-    FMA per node), not by HBM, so its FLOP rate is reported beside.  The FP64
-    SpMV of the residual replacements is reported as well."""
+    """Roofline of the kernel family with the largest share of the mixed OC
+    iteration: the FP32 matrix-free fine-level operator (four launches per
+    V-cycle plus the search-direction product), timed through the FP32
+    operator call with CUDA events on the launching stream.  Its default
+    kernel is k_mf_tc (tensor cores: tcgen05 TF32 MMAs with the 3xTF32
+    split); the FP32-FMA kernel k_mf_tile is timed beside it.  Algorithmic
+    bytes per launch: x and y (2 * 12 B per node), the fixed-DOF flags
+    (4 B per node) and the cell coefficients (4 B per cell).  The FP64 SpMV
+    of the residual replacements is reported as well."""
     import torch
     eng = opt.fem.engine
     nodes, cells = eng.mesh.nnodes, eng.mesh.nelements
     x64 = torch.rand((eng.n_dof, 1), dtype=torch.float64, device=eng.device)
     x32 = x64.float()
+    eng.set_mf_kernel(0)
+    t_fma = _event_time(lambda: eng.spmv(x32, torch.float32))
+    eng.set_mf_kernel(1)
     t32 = _event_time(lambda: eng.spmv(x32, torch.float32))
     t64 = _event_time(lambda: eng.spmv(x64))
     bytes_mf = 28 * nodes + 4 * cells
-    # DRAM traffic per launch: an ncu capture of this kernel on the 120x40x40
-    # cantilever (caches flushed) read 4.06 MB and wrote 0 B (the stores
-    # stayed in L2) for 203,401 nodes = MF_TRAFFIC_PER_NODE B per node,
-    # scaled here to this grid's node count.
+    # DRAM traffic per launch: an ncu capture of the operator on the 120x40x40
+    # cantilever (caches flushed), in bytes per node, scaled by node count
     traffic = MF_TRAFFIC_PER_NODE * nodes
     nb = eng.nnzb
     bytes64 = nb * (9 * 8 + 4) + 4 * (nodes + 1) + 2 * 8 * eng.n_dof
     achieved = bytes_mf / t32 / 1e9
-    return {"kernel": "k_mf_tile (FP32 matrix-free operator, fine level)", "bound": "hbm",
+    return {"kernel": "k_mf_tc (FP32-accurate matrix-free operator on the tensor cores, "
+                      "fine level)", "bound": "hbm",
             "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
             "frac": round(achieved / peak_gbs, 3), "bytes_per_launch": int(bytes_mf),
             "launch_us": round(t32 * 1e6, 1), "traffic": int(traffic),
-            "limiter": "FP32 FMA issue",
-            "fp32_tflops": round(2 * 576 * nodes / t32 / 1e12, 2),
+            "fp32_equiv_tflops": round(2 * 576 * nodes / t32 / 1e12, 2),
+            "fma_kernel": {"kernel": "k_mf_tile (FP32 FMA)", "launch_us": round(t_fma * 1e6, 1),
+                           "fp32_tflops": round(2 * 576 * nodes / t_fma / 1e12, 2)},
             "fp64_spmv": {"kernel": "k_sell_spmv<double,3,1> (residual replacement)",
                           "launch_us": round(t64 * 1e6, 1),
                           "achieved_gbs": round(bytes64 / t64 / 1e9, 1),
                           "bytes_per_launch": int(bytes64)}}
+
+
+FULL_ITERS = 50     # the 240x80x80 configuration's iteration count
+
+
+def per_iteration_run(opt, n_iter, check=None):
+    """Iterations 1..n_iter of `opt`, each bracketed by CUDA events on the
+    launching stream (the events see only the iteration); `check(opt)` runs
+    after each iteration, outside the events.  Returns (per-iteration ms,
+    check results)."""
+    import torch
+    s = torch.cuda.current_stream()
+    evs = []
+    out = []
+    for _ in range(n_iter):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        opt.optimize_steps(1)
+        e1.record(s)
+        evs.append((e0, e1))
+        if check is not None:
+            out.append(check(opt))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in evs], out
+
+
+def same_density_checker(opt, dev):
+    """After a mixed iteration: the FP64 solve (to 1e-10) at the iteration's
+    projected density and its sensitivity chain (dC_drho_simp x dH, filter
+    transpose), against the mixed iteration's compliance and filtered
+    sensitivity (relative error and relative L2)."""
+    import torch
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    f64 = FEM_SimpLinearElasticity(opt.tsk, 1e-9, solver_config=LinearSolverConfig(
+        solver="cg_pyamg", rtol=1e-10, precision="fp64"), device=dev)
+    U64 = torch.zeros_like(opt._state.u_dofs) if opt._state is not None else None
+
+    def check(o):
+        nonlocal U64
+        st = o._state
+        if U64 is None:
+            U64 = torch.zeros_like(st.u_dofs)
+        c64 = float(f64.solve_device(st.rho_projected, 3.0, U64)[0])
+        _, dcp = f64.sensitivity_multi_load(st.rho_projected, 3.0, U64, dh=st.dH_drho,
+                                            want_energy=False)
+        g64 = o.filter.gradient_device(dcp[:, 0].contiguous())
+        c32 = float(o.recorder.histories["compliance"][-1])
+        serr = float(torch.linalg.norm(st.dC_drho_full - g64) / torch.linalg.norm(g64))
+        return abs(c32 - c64) / abs(c64), serr
+    return check
 
 
 def run_gpu(args):
@@ -252,8 +306,9 @@ def run_gpu(args):
     size = tuple(args.size)
     peak, peak_kind = measured_peak_gbs()
     total = args.warmup + args.steps
-    # mixed precision (headline)
-    opt = make_optimizer(size, "mixed", max(50, total), dev)
+    n_full = max(FULL_ITERS, total)
+    # mixed precision (headline): W warm-up iterations, K timed
+    opt = make_optimizer(size, "mixed", n_full, dev)
     ms, wall, launches, clocks = timed_run(opt, args.warmup, args.steps, ClockSampler(local),
                                            label="mixed")
     phases = None
@@ -262,29 +317,37 @@ def run_gpu(args):
         opt.optimize_steps(2)
         opt.timer.enabled = False
         phases = opt.timer.report()
-    comp_mixed = list(opt.recorder.histories["compliance"])
     mixed_stats = [(s.iters, s.outer, s.relres) for s in opt.fem.solve_history]
     roof = roofline(opt, peak)
-    # same-density check: FP64 solve on the final mixed design
-    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
-    f64 = FEM_SimpLinearElasticity(opt.tsk, 1e-9, solver_config=LinearSolverConfig(
-        solver="cg_pyamg", rtol=1e-10, precision="fp64"), device=dev)
-    st = opt._state
-    U64 = torch.zeros_like(st.u_dofs)
-    c64 = float(f64.solve_device(st.rho_projected, 3.0, U64)[0])
-    U32 = torch.zeros_like(st.u_dofs)
-    c32 = float(opt.fem.solve_device(st.rho_projected, 3.0, U32)[0])
-    same_density_err = abs(c32 - c64) / abs(c64)
-    del f64
     n = opt.tsk.mesh.nelements
     del opt
     torch.cuda.empty_cache()
+    # all iterations of the configuration, mixed, each against the FP64 solve
+    # and sensitivity chain at the same density
+    full = None
+    comp_mixed = None
+    if not args.no_fp64:
+        om = make_optimizer(size, "mixed", n_full, dev)
+        om._ensure_state_initialized()
+        om.fem.engine                     # set-up outside the timed iterations
+        t_mixed, errs = per_iteration_run(om, n_full, same_density_checker(om, dev))
+        comp_mixed = list(om.recorder.histories["compliance"])
+        full = {"iterations": n_full, "mixed_it_per_s": round(n_full / (sum(t_mixed) * 1e-3), 4),
+                "mixed_ms_per_iter": [round(t, 2) for t in t_mixed],
+                "compliance_rel_err_same_density": [float(f"{e[0]:.3e}") for e in errs],
+                "sensitivity_rel_l2_err_same_density": [float(f"{e[1]:.3e}") for e in errs],
+                "compliance_rel_err_same_density_max": max(e[0] for e in errs),
+                "sensitivity_rel_l2_err_same_density_max": max(e[1] for e in errs),
+                "mixed_solver_iters": [(s.iters, s.outer) for s in om.fem.solve_history],
+                "_t_mixed": t_mixed}
+        del om
+        torch.cuda.empty_cache()
     # e2e: the same iterations (same start, same warm-up) through the
     # host-buffer call path: density from pinned host memory in, density and
     # compliance back out, every step
     e2e = None
     if not args.no_e2e:
-        oe = make_optimizer(size, "mixed", max(50, total), dev)
+        oe = make_optimizer(size, "mixed", n_full, dev)
         rho_h = torch.empty(n, dtype=torch.float64).pin_memory()
         oe.optimize_steps(1)                  # state initialised
         rho_h.copy_(oe._state.rho)
@@ -299,18 +362,27 @@ def run_gpu(args):
                "h2d_bytes_per_step": 8 * n, "d2h_bytes_per_step": 8 * n + 8}
         del oe
         torch.cuda.empty_cache()
-    # plain FP64 run from the same start
+    # plain FP64 path from the same start: the K-step window and all iterations
     fp64 = None
     if not args.no_fp64:
-        o64 = make_optimizer(size, "fp64", max(50, total), dev)
-        ms64, wall64, _, _ = timed_run(o64, args.warmup, args.steps, label="fp64")
+        o64 = make_optimizer(size, "fp64", n_full, dev)
+        o64._ensure_state_initialized()
+        o64.fem.engine
+        t64, _ = per_iteration_run(o64, n_full)
+        ms64 = sum(t64[args.warmup:total])          # the same K-step window
         comp64 = list(o64.recorder.histories["compliance"])
         errs = [abs(a - b) / abs(b) for a, b in zip(comp_mixed, comp64)]
-        fp64 = {"value": round(args.steps / (ms64 * 1e-3), 4), "ms_per_step": round(ms64 / args.steps, 2),
+        fp64 = {"value": round(args.steps / (ms64 * 1e-3), 4),
+                "ms_per_step": round(ms64 / args.steps, 2),
                 "compliance_rel_err_max": max(errs), "compliance_rel_err_per_iter": errs,
                 "speedup_mixed_vs_fp64": round(ms64 / ms, 3),
                 "solver_iters": [(s.iters, s.relres) for s in o64.fem.solve_history][-args.steps:]}
+        full["fp64_it_per_s"] = round(n_full / (sum(t64) * 1e-3), 4)
+        full["fp64_ms_per_iter"] = [round(t, 2) for t in t64]
+        full["speedup_mixed_vs_fp64"] = round(sum(t64) / sum(full["_t_mixed"]), 3)
         del o64
+    if full is not None:
+        full.pop("_t_mixed", None)
     # max over ranks
     t_step = replica_max(ms * 1e-3)
     value = args.steps / t_step * world
@@ -332,7 +404,7 @@ def run_gpu(args):
         "e2e": e2e, "gpu_launches": int(launches),
         "roofline": dict(roof, peak_kind=peak_kind),
         "fp64_path": fp64,
-        "compliance_rel_err_same_density": same_density_err,
+        "all_iterations": full,
         "mixed_solver_iters": mixed_stats[-args.steps:],
         "clocks": clocks,
     }

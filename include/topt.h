@@ -121,6 +121,18 @@ int topt_fem_set_interpolation(topt_fem* h, int32_t kind);
  * available on handles with the matrix-free FP32 operator. */
 int topt_fem_set_element_extra(topt_fem* h, const double* extra);
 
+/* Kernel of the matrix-free FP32 level-0 operator (handles created with
+ * mf_level0 on a uniform hex grid): 1 = tensor cores (tcgen05, TF32 with the
+ * 3xTF32 split, FP32-accurate; the default), 0 = FP32 FMA tiles.  Both compute
+ * the same operator (the element products of composer.py:53-101 on one unit
+ * matrix, enforce as identity rows); they differ by rounding only.
+ * mf_error (may be NULL) receives 1 if a tensor-core launch gave up on one
+ * of its bounded waits (the operator then also wrote a NaN into its output,
+ * so the solve ends with TOPT_NONFINITE).  No reference counterpart: the
+ * reference assembles with scikit-fem and multiplies with SciPy. */
+int topt_fem_set_mf_kernel(topt_fem* h, int32_t kind);
+int topt_fem_mf_error(topt_fem* h, int32_t* mf_error);
+
 typedef struct topt_solve_opts {
   int32_t method;         /* 0: FP64 PCG.  Mixed (FP32 operator, hierarchy and
                              inner work; FP64 residual, update and dots):

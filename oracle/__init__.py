@@ -9,23 +9,26 @@ follows (paths are relative to the reference project root).
 
 Parity status
 -------------
-* The reference cannot be imported here: scikit-fem, PyAMG and numba are
-  not installed and there is no network.  The third-party arithmetic the
-  reference delegates to is restated from its published behaviour:
-
-  - scikit-fem 11.x (pyproject.toml:18): ``MeshHex.init_tensor`` node and
-    element numbering, ``ElementHex1`` / ``ElementTetP1`` bases with exact
-    Gauss quadrature, ``asm`` COO->CSR with duplicates summed and sorted
-    columns, ``enforce`` (rows and columns of the Dirichlet DOFs zeroed,
-    unit diagonal, RHS set to the prescribed value), ``condense``/``solve``.
-  - SciPy 1.18 (present here): ``spsolve``, ``splu``, ``cg``, ``cKDTree``.
-
-* The reference's own tests pin no numerical results (they check
-  ``isfinite`` and stepwise self-consistency only).  The oracle is pinned
-  against the known answers of ``scikit-topt/tests/test_scheduler.py`` and
-  against analytic properties (rigid-body null space of element matrices,
-  exact volumes, symmetric positive definiteness, filter row sums, finite
-  differences).  Everything at the scikit-fem boundary is therefore
-  **parity unpinned**: it follows the restatement, not a run of the
-  reference.
+* Pinned to the reference's own code: everything the reference computes
+  with NumPy/SciPy itself.  ``tests/golden/make_ref_fixtures.py`` imports the
+  unmodified reference sources (inert stand-ins replace the missing
+  scikit-fem, PyAMG, numba, matplotlib and meshio) and writes fixtures from
+  its projection, derivatives, interpolation and volumes, orientation fixes,
+  element sets, schedules, Gaussian filter, OC bisection, log update, both
+  ``rho_update`` hooks and whole runs of its driver loop
+  (``DensityMethod._optimize_impl``) with this oracle's FEM plugin;
+  ``tests/test_cpu_ref_pinned.py`` checks this package against them.
+* Parity unpinned: the arithmetic the reference delegates to scikit-fem
+  11.x (pyproject.toml:18), restated here from its published behaviour --
+  ``MeshHex.init_tensor`` node and element numbering, ``ElementHex1`` /
+  ``ElementTetP1`` bases with exact Gauss quadrature, ``asm`` COO->CSR with
+  duplicates summed and sorted columns, ``enforce`` (rows and columns of the
+  Dirichlet DOFs zeroed, unit diagonal, RHS set to the prescribed value),
+  ``condense``/``solve``, facet integrals, the nodal Helmholtz system.  Those
+  parts are pinned by analytic properties (rigid-body null space of element
+  matrices, exact volumes, symmetric positive definiteness, filter row
+  sums, finite differences) and by fixtures of this restatement
+  (``tests/golden/make_golden.py``).
+* SciPy 1.18 (present here) supplies ``spsolve``, ``splu``, ``cg`` and
+  ``cKDTree`` as in the reference.
 """

@@ -122,6 +122,7 @@ class OracleConfig:
     solver: str = "spsolve"
     interpolation: str = "SIMP"        # "SIMP" | "RAMP" (common_density.py:392-404)
     rtol: float = 1e-8
+    sensitivity_filter: bool = False   # common_density.py:1102-1106
 
     def __post_init__(self):
         if self.eta is None:
@@ -202,6 +203,8 @@ class OracleOptimizer:
                                                          Emin, p)
             dC_full += self.filt.gradient(dCp * dH)
         dC_full /= U.shape[1]
+        if cfg.sensitivity_filter:
+            dC_full = self.filt.forward(dC_full)
         dC_d = dC_full[self.design].copy()
         rho_d = self.rho[self.design].copy()
         if cfg.method == "oc":

@@ -10,6 +10,7 @@
 // grid (Galerkin coarse operators built element by element, Chebyshev
 // smoothing, dense coarsest solve).
 #include "fem_kernels.cuh"
+#include "mf_tc.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -119,7 +120,12 @@ struct topt_fem {
   bool mf = false;
   topt::MfGrid mfg{};
   int mf_ty = 32;                      // y extent of the operator's node tiles
-  float k0_host[576] = {};             // FP32 unit matrix (constant-bank copy)
+  topt::K0f k0{};                      // FP32 unit matrix (by-value kernel parameter)
+  // tensor-core operator (k_mf_tc): 0 = FP32-FMA tiles (k_mf_tile), 1 = tcgen05
+  int mf_kernel = 1;
+  topt::MfTcGrid mftc{};
+  topt::DevBuf k0img;                  // K0 hi / lo in the MMA operand layout
+  topt::DevBuf mf_err;                 // set by k_mf_tc if an mbarrier wait times out
   topt::DevBuf nmask32;                // nmask widened to 32 bits (cp.async granule)
   topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
 };
@@ -360,17 +366,6 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
 }
 
 // MODE 0 y=Ax, 1 y=b-Ax, 2 y-=Ax; dot -> red slot
-// The single-load matrix-free kernel reads K0 from constant memory; the
-// constant bank is per process, so it is (re)loaded on the handle's stream
-// whenever another handle's K0 was loaded last.
-// The bank is process-wide: handles whose K0 has the same contents share it;
-// a handle with different contents reloads it (under g_k0_mu).  Concurrent
-// handles on different streams must therefore share K0 (uniform grids of the
-// same cell size do); the batched driver checks this.
-static std::mutex g_k0_mu;
-static float g_k0_host[576];
-static int g_k0_dev = -1;
-
 template <int TY, int MODE, bool DOT, bool COLMASK>
 static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y, int slot) {
   static bool attr_set = false;   // per instantiation, process-wide
@@ -382,9 +377,83 @@ static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y,
   }
   k_mf_tile<TY, MODE, DOT, COLMASK><<<h->sm * kMfCtasPerSm, kMfThreads, MfTile<TY>::SMEM,
                                       h->stream>>>(
-      h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), x, b, y,
+      h->mfg, h->k0, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), x, b, y,
       h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot));
   TOPT_CHECK_LAUNCH("k_mf_tile");
+  return TOPT_OK;
+}
+
+// Tensor-core variant: persistent, two CTAs per SM over (column, z segment)
+// work items.
+template <int MODE, bool DOT, bool COLMASK>
+static int launch_mf_tc(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  static bool attr_set = false;   // per instantiation, process-wide
+  if (!attr_set) {
+    TOPT_CUDA(cudaFuncSetAttribute(k_mf_tc<MODE, DOT, COLMASK>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)mftc::SMEM));
+    attr_set = true;
+  }
+  const MfTcGrid& G = h->mftc;
+  const int64_t items = (int64_t)G.ncy * G.ncx * G.nseg;
+  const int grid = (int)std::min<int64_t>(items, (int64_t)h->sm * 2);
+  k_mf_tc<MODE, DOT, COLMASK><<<grid, mftc::THREADS, mftc::SMEM, h->stream>>>(
+      G, h->k0img.as<float>(), h->coef32.as<float>(), h->nmask32.as<uint32_t>(), x, b, y,
+      h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot),
+      h->mf_err.as<int>());
+  TOPT_CHECK_LAUNCH("k_mf_tc");
+  return TOPT_OK;
+}
+
+// Round to TF32 (10-bit mantissa), nearest with ties away from zero: the
+// rounding of cvt.rna.tf32.f32, for the host-built K0 image.
+static float tf32_rna_host(float v) {
+  uint32_t u;
+  std::memcpy(&u, &v, 4);
+  if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+
+// K0 split into TF32 hi and lo parts, rows padded to N = 32, in the K-major
+// operand layout of k_mf_tc; and the column / z-segment decomposition that
+// balances the work items over two CTAs per SM.
+static int setup_mf_tc(topt_fem* h, cudaStream_t s) {
+  std::vector<float> img(mftc::K0_IMAGE_FLOATS, 0.0f);
+  for (int n = 0; n < 32; ++n)
+    for (int k = 0; k < 24; ++k) {
+      const float v = n < 24 ? h->k0.v[n * 24 + k] : 0.0f;
+      const float hi = tf32_rna_host(v);
+      const float lo = tf32_rna_host(v - hi);
+      const uint32_t o = tc::kmaj_off(n, k, mftc::SBO_B) / 4;
+      img[o] = hi;
+      img[32 * 24 + o] = lo;
+    }
+  int rc = upload(h->k0img, img.data(), img.size(), s);
+  if (rc) return rc;
+  if ((rc = h->mf_err.alloc(sizeof(int)))) return rc;
+  TOPT_CUDA(cudaMemsetAsync(h->mf_err.p, 0, sizeof(int), s));
+  MfTcGrid& G = h->mftc;
+  G.g = h->mfg;
+  const int ny1 = h->mfg.ny + 1, nx1 = h->mfg.nx + 1, nz1 = h->mfg.nz + 1;
+  G.ncy = (ny1 + mftc::NY - 1) / mftc::NY;
+  G.ncx = (nx1 + mftc::NX - 1) / mftc::NX;
+  const int64_t cols = (int64_t)G.ncy * G.ncx, slots = (int64_t)h->sm * 2;
+  int64_t best = -1;
+  for (int nseg = 1; nseg <= nz1; ++nseg) {
+    const int zs = (nz1 + nseg - 1) / nseg;
+    const int used = (nz1 + zs - 1) / zs;
+    const int64_t items = cols * used;
+    const int64_t waves = (items + slots - 1) / slots;
+    const int64_t cost = waves * (zs + 2);
+    if (best < 0 || cost < best) {
+      best = cost;
+      G.nseg = used;
+      G.zs = zs;
+    }
+  }
+  TOPT_CUDA(cudaStreamSynchronize(s));
   return TOPT_OK;
 }
 
@@ -399,24 +468,17 @@ template <int L, int MODE, bool DOT>
 static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int slot,
                      const ChebEp<float>& ep, bool zero_fixed) {
   if (L == 1) {
-    {
-      std::lock_guard<std::mutex> lk(g_k0_mu);
-      int dev = 0;
-      TOPT_CUDA(cudaGetDevice(&dev));
-      if (g_k0_dev != dev || std::memcmp(g_k0_host, h->k0_host, sizeof(g_k0_host)) != 0) {
-        TOPT_CUDA(cudaMemcpyToSymbolAsync(c_K0f, h->k0_host, 576 * sizeof(float), 0,
-                                          cudaMemcpyHostToDevice, h->stream));
-        TOPT_CUDA(cudaStreamSynchronize(h->stream));
-        std::memcpy(g_k0_host, h->k0_host, sizeof(g_k0_host));
-        g_k0_dev = dev;
-      }
-    }
-    const int rc = zero_fixed ? launch_mf_ty<MODE, DOT, false>(h, x, b, y, slot)
-                              : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
+    int rc;
+    if (h->mf_kernel == 1)
+      rc = zero_fixed ? launch_mf_tc<MODE, DOT, false>(h, x, b, y, slot)
+                      : launch_mf_tc<MODE, DOT, true>(h, x, b, y, slot);
+    else
+      rc = zero_fixed ? launch_mf_ty<MODE, DOT, false>(h, x, b, y, slot)
+                      : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
     if (rc) return rc;
     if (ep.kind) {
       k_cheb_mf<<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
-          h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, y);
+          h->mfg, h->k0, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, y);
       TOPT_CHECK_LAUNCH("k_cheb_mf");
     }
     return TOPT_OK;
@@ -939,7 +1001,8 @@ static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b
       ep.dnew = (float*)N.d.p;
       ep.x = (float*)x;
       k_cheb_mf<<<gridsize(h, Ls.n_nodes), kBlock, 0, h->stream>>>(
-          h->mfg, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, (const float*)b);
+          h->mfg, h->k0, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep,
+          (const float*)b);
       TOPT_CHECK_LAUNCH("k_cheb_mf");
     } else {
       TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
@@ -999,14 +1062,33 @@ static int precond_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int p
   return TOPT_OK;
 }
 
-// Zero the fixed DOFs of an initial guess (FP64 solution vectors; the FP32
-// hierarchy is never started from a guess).
+// Columns j with bit j of `cols` set are zeroed (n x L row-major).
 template <typename T>
-static int start_from(topt_fem* h, int L, T* x) {
+__global__ void k_zero_cols(int64_t n, int L, unsigned cols, T* __restrict__ x) {
+  TOPT_KERNEL_COUNT();
+  const int64_t nl = n * L;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nl;
+       i += (int64_t)gridDim.x * blockDim.x)
+    if ((cols >> (int)(i % L)) & 1u) x[i] = T(0);
+}
+
+// Zero the fixed DOFs of an initial guess (FP64 solution vectors; the FP32
+// hierarchy is never started from a guess), and the whole column of every
+// load case whose right-hand side vanishes (active_h[j] == 0): such a column
+// takes no iteration, so its solution is the zero vector, not the guess.
+template <typename T>
+static int start_from(topt_fem* h, int L, T* x, const int* active_h) {
   if (std::is_same<T, double>::value) {
     k_zero_fixed<<<gridsize(h, h->n_dof * L), kBlock, 0, h->stream>>>(
         h->n_dof, L, h->mask.as<uint8_t>(), (double*)x);
     TOPT_CHECK_LAUNCH("k_zero_fixed");
+  }
+  unsigned cols = 0;
+  for (int j = 0; j < L; ++j)
+    if (!active_h[j]) cols |= 1u << j;
+  if (cols) {
+    k_zero_cols<T><<<gridsize(h, h->n_dof * L), kBlock, 0, h->stream>>>(h->n_dof, L, cols, x);
+    TOPT_CHECK_LAUNCH("k_zero_cols");
   }
   return TOPT_OK;
 }
@@ -1121,17 +1203,17 @@ static int pcg(topt_fem* h, Hier<T>& H, int L, const T* b, T* x, T* p, T* q, T* 
   double bnorm2[4] = {0, 0, 0, 0};
   if ((rc = dot<T>(h, n, L, b, b, 2))) return rc;
   if ((rc = read_slot(h, 2, L, bnorm2))) return rc;
+  // device scalars: slots 3 (rz A), 4 (rz B), 5 (pq), 6 (rr); active flags
+  int active_h[4] = {1, 1, 1, 1};
+  for (int j = 0; j < L; ++j)
+    if (!(bnorm2[j] > 0.0)) active_h[j] = 0;
   if (x0) {   // r = b - A x from the caller's x (fixed DOFs zeroed first)
-    if ((rc = start_from(h, L, x))) return rc;
+    if ((rc = start_from(h, L, x, active_h))) return rc;
     if ((rc = spmv<T>(h, L0, bs, L, 1, false, vals, x, b, r))) return rc;
   } else {
     TOPT_CUDA(cudaMemsetAsync(x, 0, sizeof(T) * nl, h->stream));
     TOPT_CUDA(cudaMemcpyAsync(r, b, sizeof(T) * nl, cudaMemcpyDeviceToDevice, h->stream));
   }
-  // device scalars: slots 3 (rz A), 4 (rz B), 5 (pq), 6 (rr); active flags
-  int active_h[4] = {1, 1, 1, 1};
-  for (int j = 0; j < L; ++j)
-    if (!(bnorm2[j] > 0.0)) active_h[j] = 0;
   DevBuf& active = h->active;
   TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
                             h->stream));
@@ -1207,7 +1289,7 @@ static int pcg_fcg_mixed(topt_fem* h, int L, double* U, double* p, double* q, do
   TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
                             h->stream));
   if (h->x0) {   // r = Fe - K U from the caller's U (fixed DOFs zeroed first)
-    if ((rc = start_from<double>(h, L, U))) return rc;
+    if ((rc = start_from<double>(h, L, U, active_h))) return rc;
     if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r))) return rc;
   } else {
     TOPT_CUDA(cudaMemsetAsync(U, 0, sizeof(double) * nl, h->stream));
@@ -1304,7 +1386,7 @@ static int pcg_fcg_rr(topt_fem* h, int L, double* U, double* r64, float* p32, fl
   TOPT_CUDA(cudaMemcpyAsync(active.p, active_h, 4 * sizeof(int), cudaMemcpyHostToDevice,
                             h->stream));
   if (h->x0) {   // r = Fe - K U from the caller's U (fixed DOFs zeroed first)
-    if ((rc = start_from<double>(h, L, U))) return rc;
+    if ((rc = start_from<double>(h, L, U, active_h))) return rc;
     if ((rc = spmv<double>(h, L0, bs, L, 1, false, A64, U, fe, r64))) return rc;
     if ((rc = dot<double>(h, n, L, r64, r64, 7))) return rc;
     if ((rc = read_slot(h, 7, L, rlast2))) return rc;
@@ -1431,7 +1513,7 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
     std::vector<float> k32(d->ke, d->ke + nke);
     if ((rc = upload(h->ke32, k32.data(), nke, s))) return rc;
     TOPT_CUDA(cudaStreamSynchronize(s));
-    if (nke == 576) std::copy(k32.begin(), k32.end(), h->k0_host);
+    if (nke == 576) std::copy(k32.begin(), k32.end(), h->k0.v);
   }
   if ((rc = upload(h->mask, d->dirichlet, (size_t)h->n_dof, s))) return rc;
   if ((rc = h->coef64.alloc(sizeof(double) * d->n_elem))) return rc;
@@ -1501,6 +1583,7 @@ int topt_fem_create(const topt_fem_desc* d, topt_fem** out) {
       }
       TOPT_CUDA(cudaStreamSynchronize(s));
       h->mf_ty = mf_pick_ty(ny + 1);
+      if ((rc = setup_mf_tc(h.get(), s))) return rc;
     }
     if (h->ls.size() > 1) {
       LevelStruct& B = h->ls.back();
@@ -1543,6 +1626,24 @@ int topt_fem_sizes(const topt_fem* h, int64_t* n_dof, int64_t* nnzb, int32_t* n_
   if (n_dof) *n_dof = h->n_dof;
   if (nnzb) *nnzb = h->ls[0].nnzb;
   if (n_levels) *n_levels = (int32_t)h->ls.size();
+  return TOPT_OK;
+}
+
+int topt_fem_set_mf_kernel(topt_fem* h, int32_t kind) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_mf_kernel: null handle");
+  if (kind < 0 || kind > 1)
+    return fail(TOPT_BAD_INPUT, "fem_set_mf_kernel: kind must be 0 (FMA) or 1 (tensor cores)");
+  h->mf_kernel = kind;
+  return TOPT_OK;
+}
+
+int topt_fem_mf_error(topt_fem* h, int32_t* mf_error) {
+  if (!h || !mf_error) return fail(TOPT_BAD_INPUT, "fem_mf_error: null argument");
+  *mf_error = 0;
+  if (h->mf_err.p) {
+    TOPT_CUDA(cudaStreamSynchronize(h->stream));
+    TOPT_CUDA(cudaMemcpy(mf_error, h->mf_err.p, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
   return TOPT_OK;
 }
 

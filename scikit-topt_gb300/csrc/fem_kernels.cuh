@@ -393,12 +393,17 @@ k_mf_apply(MfGrid g, const T* __restrict__ K0, const T* __restrict__ coef,
   }
 }
 
-// Single-load operator: the unit matrix sits in constant memory and every
-// loop index is a compile-time constant, so each of the 576 FMAs per node
-// reads its K0 operand straight from the constant bank.  nmask packs the
-// fixed flags of a node's three DOFs in bits 0-2; hoff(a, d) is the offset of
-// local node a along axis d (MeshHex order).
-__constant__ float c_K0f[576];
+// Single-load operator: the unit matrix is passed by value as a kernel
+// parameter (2,304 B, parameter space of the launch, so concurrent handles
+// with different matrices never share it) and every loop index is a
+// compile-time constant, so each of the 576 FMAs per node reads its K0
+// operand straight from the constant bank.  nmask packs the fixed flags of a
+// node's three DOFs in bits 0-2; hoff(a, d) is the offset of local node a
+// along axis d (MeshHex order).
+struct K0f {
+  float v[576];
+  __host__ __device__ float operator[](int i) const { return v[i]; }
+};
 
 __host__ __device__ constexpr int hoff(int a, int d) {
   return d == 0 ? (0xD4 >> a) & 1 : (d == 1 ? (0xB2 >> a) & 1 : (0xE8 >> a) & 1);
@@ -511,9 +516,10 @@ __device__ __forceinline__ void mf_stage(float* buf, int t, const MfGrid& g, int
 
 template <int TY, int MODE, bool DOT, bool COLMASK>
 __global__ void __launch_bounds__(kMfThreads, kMfCtasPerSm)
-k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint32_t* __restrict__ m32,
-          const float* __restrict__ x, const float* __restrict__ b, float* __restrict__ y,
-          double* partials, unsigned* counter, double* dot_out) {
+k_mf_tile(MfGrid g, const K0f k0, const float* __restrict__ coef,
+          const uint32_t* __restrict__ m32, const float* __restrict__ x,
+          const float* __restrict__ b, float* __restrict__ y, double* partials,
+          unsigned* counter, double* dot_out) {
   TOPT_KERNEL_COUNT();
   using G = MfTile<TY>;
   constexpr int TX = kMfTX, TZ = kMfTZ, NT = kMfThreads, HY = G::HY, HX = G::HX;
@@ -567,7 +573,7 @@ k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint32_t* __restrict__
           for (int c = 0; c < 3; ++c)
 #pragma unroll
             for (int d = 0; d < 3; ++d)
-              part[c] = fmaf(c_K0f[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
+              part[c] = fmaf(k0.v[(3 * la + c) * 24 + 3 * lb + d], xv[d], part[c]);
         }
         const float s = cs[((lz + 1 - hoff(la, 2)) * CX + (lx + 1 - hoff(la, 0))) * CY +
                            (ly + 1 - hoff(la, 1))];
@@ -601,9 +607,9 @@ k_mf_tile(MfGrid g, const float* __restrict__ coef, const uint32_t* __restrict__
 // Inverted 3x3 diagonal block of node (ix, iy, iz) of the matrix-free
 // operator (block Jacobi): D = sum_c coef_c K0[la, la] over the <= 8 cells
 // around the node, fixed DOFs (bits of m) as identity rows / columns; FP32.
-// K0 comes from the constant bank (CONSTK) or from memory.
-template <bool CONSTK>
-__device__ __forceinline__ void mf_node_dinv(const MfGrid& g, const float* __restrict__ K0,
+// K0 is the by-value parameter (K0f) or a pointer to memory.
+template <class KS>
+__device__ __forceinline__ void mf_node_dinv(const MfGrid& g, const KS& K0,
                                              const float* __restrict__ coef, int m, int ix,
                                              int iy, int iz, float* O) {
   float D[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
@@ -617,7 +623,7 @@ __device__ __forceinline__ void mf_node_dinv(const MfGrid& g, const float* __res
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const int k = (3 * la + c) * 24 + 3 * la + d;
-        D[c * 3 + d] += s * (CONSTK ? c_K0f[k] : K0[k]);
+        D[c * 3 + d] += s * K0[k];
       }
   }
   if (m) {
@@ -654,7 +660,7 @@ __global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
     const int ai = (int)a;  // node counts fit 32 bits: cheap index math
     const int iy = ai % ny1, ix = (ai / ny1) % nx1, iz = ai / (ny1 * nx1);
     const int m = mask ? (mask[a * 3] | (mask[a * 3 + 1] << 1) | (mask[a * 3 + 2] << 2)) : 0;
-    mf_node_dinv<false>(g, K0, coef, m, ix, iy, iz, dinv + a * 9);
+    mf_node_dinv(g, K0, coef, m, ix, iy, iz, dinv + a * 9);
   }
 }
 
@@ -662,7 +668,7 @@ __global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
 // inverted diagonal block is recomputed per node from the cell coefficients
 // (the same FP32 arithmetic as k_mf_diag_inv, so the same bits) instead of
 // being read, which saves 36 B per node.  m32: fixed-DOF bits per node.
-__global__ void k_cheb_mf(MfGrid g, const float* __restrict__ coef,
+__global__ void k_cheb_mf(MfGrid g, const K0f k0, const float* __restrict__ coef,
                           const uint32_t* __restrict__ m32, ChebEp<float> ep,
                           const float* __restrict__ r) {
   TOPT_KERNEL_COUNT();
@@ -672,7 +678,7 @@ __global__ void k_cheb_mf(MfGrid g, const float* __restrict__ coef,
     const int iy = a % ny1, ix = (a / ny1) % nx1, iz = a / (ny1 * nx1);
     float rv[3] = {r[(int64_t)a * 3], r[(int64_t)a * 3 + 1], r[(int64_t)a * 3 + 2]};
     float Dv[9];
-    mf_node_dinv<true>(g, nullptr, coef, (int)m32[a], ix, iy, iz, Dv);
+    mf_node_dinv(g, k0, coef, (int)m32[a], ix, iy, iz, Dv);
     cheb_update<float, 3, 1>(ep, a, rv, Dv);
   }
 }

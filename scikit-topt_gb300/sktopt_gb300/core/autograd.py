@@ -7,6 +7,8 @@ a composition of ``torch.autograd.Function`` objects whose backward passes
 call the GPU kernels:
 
 * ``GaussianFilterFn``: forward W rho (design rows), backward W^T g;
+* ``HelmholtzFilterFn``: forward the nodal Helmholtz filter, backward its
+  exact transpose (not the reference's clamped ``gradient``);
 * ``ProjectionFn``: forward H(x), backward H'(x) g (projection.py:27-118);
 * ``ComplianceFn``: forward solves K(rho) U = F and returns sum_j F_j . U_j
   (elasticity) or T^T K T (conduction); only U is saved, the element strains
@@ -65,6 +67,17 @@ class GaussianFilterFn(torch.autograd.Function):
         return ctx.flt.gradient_device(g.contiguous()), None
 
 
+class HelmholtzFilterFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, flt):
+        ctx.flt = flt
+        return flt.forward_device(x.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, g):
+        return ctx.flt.vjp_device(g.contiguous()), None
+
+
 def compliance(rho: torch.Tensor, fem, p: float = 3.0) -> torch.Tensor:
     """Compliance (sum over load cases) of the physical density ``rho``."""
     return ComplianceFn.apply(rho, fem, p)
@@ -72,6 +85,7 @@ def compliance(rho: torch.Tensor, fem, p: float = 3.0) -> torch.Tensor:
 
 def filtered_compliance(rho: torch.Tensor, fem, flt, p: float = 3.0, beta: float = 1.0,
                         eta: float = 0.5) -> torch.Tensor:
-    """Compliance of H(W rho): the objective the OC loop differentiates."""
-    return ComplianceFn.apply(ProjectionFn.apply(GaussianFilterFn.apply(rho, flt), beta, eta),
-                              fem, p)
+    """Compliance of H(F rho), F the Gaussian or the Helmholtz filter: the
+    objective the OC loop differentiates."""
+    Fn = HelmholtzFilterFn if hasattr(flt, "vjp_device") else GaussianFilterFn
+    return ComplianceFn.apply(ProjectionFn.apply(Fn.apply(rho, flt), beta, eta), fem, p)

@@ -102,14 +102,16 @@ def partition_designs(costs, world_size: int) -> list:
 
 def gather_design_results(local: dict, group=None) -> dict | None:
     """The one collective of a sharded batch: every rank's {design index:
-    result} is gathered on rank 0 (None elsewhere); a single process
-    returns its own results."""
+    result} is gathered on the group's rank 0 (None elsewhere); a single
+    process returns its own results.  ``group`` may be any process group:
+    the destination is the global rank of its first member."""
     import torch.distributed as dist
     if not (dist.is_available() and dist.is_initialized()):
         return dict(local)
     world = dist.get_world_size(group)
+    dst = 0 if group is None else dist.get_global_rank(group, 0)
     out = [None] * world if dist.get_rank(group) == 0 else None
-    dist.gather_object(local, out, dst=0, group=group)
+    dist.gather_object(local, out, dst=dst, group=group)
     if out is None:
         return None
     merged = {}

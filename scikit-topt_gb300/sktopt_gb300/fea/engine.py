@@ -99,6 +99,16 @@ class FemEngine:
         later update / energy calls."""
         N.check(self.lib.topt_fem_set_interpolation(self.h, int(kind)))
 
+    def set_mf_kernel(self, kind: int):
+        """Kernel of the matrix-free FP32 level-0 operator: 1 tensor cores
+        (default), 0 FP32 FMA tiles."""
+        N.check(self.lib.topt_fem_set_mf_kernel(self.h, int(kind)))
+
+    def mf_error(self) -> int:
+        out = C.c_int32(0)
+        N.check(self.lib.topt_fem_mf_error(self.h, C.byref(out)))
+        return out.value
+
     def set_extra(self, extra: torch.Tensor | None):
         """Per-element matrices (n_e, nd, nd) added to the level-0 operator
         from the next update on; the tensor must stay alive (None removes)."""

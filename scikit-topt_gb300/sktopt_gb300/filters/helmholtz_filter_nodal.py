@@ -10,7 +10,13 @@ Drop-in for ``HelmholtzFilterNodal`` (sktopt/filters/helmholtz_filter_nodal.py:
 * gradient: the same average with non-design elements counting as 0, a pure
   Neumann solve, node -> element mean and the reference's clamp to <= 0
   (helmholtz_filter_nodal.py:200-233).  Like the reference, ``gradient`` is
-  not the exact transpose of ``forward``.
+  not the exact transpose of ``forward``;
+* vjp: the exact transpose of forward's linear part (the derivative of the
+  filtered density with respect to the design densities), for gradients
+  that must pass a finite-difference check: v -> node sums v_e / nloc ->
+  solve with the non-design nodes held at 0 -> M -> element e gets
+  vol_e sum over its nodes n of (M z)_n / wsum_n, wsum_n the volume of the
+  elements around n (zero on non-design elements).
 
 The nodal systems are solved on the GPU by multigrid-preconditioned CG to a
 relative residual of 1e-12 (the reference uses a direct solver).
@@ -68,6 +74,20 @@ class HelmholtzFilterNodal(DesignOps, BaseFilter):
         self._fixed_mask = np.zeros(nn, np.uint8)
         self._fixed_mask[fixed_nodes] = 1
         self._x0 = torch.from_numpy(self._fixed_mask.astype(np.float64)[:, None]).to(dev)
+        # for the exact transpose: elements per node / nloc, the volume of the
+        # elements around each node, and vol_e * nloc on design elements
+        cnt = np.zeros(nn)
+        wsum = np.zeros(nn)
+        np.add.at(cnt, t.ravel(), 1.0)
+        np.add.at(wsum, t.ravel(), np.repeat(self.elements_volume[None, :], t.shape[0],
+                                             axis=0).ravel())
+        self._cnt_nloc = torch.from_numpy((cnt / t.shape[0])[:, None]).to(dev)
+        self._inv_wsum = torch.from_numpy(
+            np.where(wsum > 0, 1.0 / np.where(wsum > 0, wsum, 1.0), 0.0)[:, None]).to(dev)
+        self._vol_nloc_design = torch.from_numpy(
+            np.where(dmask, self.elements_volume * t.shape[0], 0.0)).to(dev)
+        self._ones_e = torch.ones(ne, dtype=torch.float64, device=dev)
+        self._all_design = torch.ones(ne, dtype=torch.uint8, device=dev)
         _, self._Kh, self._M = composer.element_matrices(mesh, 0.3)
         self._eng = None
         self.radius = None
@@ -130,6 +150,24 @@ class HelmholtzFilterNodal(DesignOps, BaseFilter):
         out = torch.empty_like(v) if out is None else out
         b = self._eng_M.spmv(self._e2n(v.contiguous(), 0.0))
         return self._n2e(self._solve(self._eng_free, b), True, out)
+
+    def vjp_device(self, v, out=None):
+        """Exact transpose of forward_device's linear part, applied to v."""
+        out = torch.empty_like(v) if out is None else out
+        # w_n = sum over the elements e around n of v_e / nloc: the unweighted
+        # average over all of them, times their count / nloc
+        wn = torch.empty((self.mesh.nnodes, 1), dtype=torch.float64, device=self.device)
+        N.check(self.lib.topt_elem_to_node(self.mesh.nnodes, _p(self._nptr), _p(self._nel),
+                                           _p(self._ones_e), _p(v.contiguous()),
+                                           _p(self._all_design), 0.0, _p(wn),
+                                           C.c_void_p(stream_handle())))
+        wn *= self._cnt_nloc
+        z = self._solve(self._eng_fixed if self._eng_fixed is not None else self._eng_free, wn)
+        u = self._eng_M.spmv(z)
+        u *= self._inv_wsum
+        self._n2e(u, False, out)
+        out *= self._vol_nloc_design
+        return out
 
     def forward(self, rho_element):
         x = as_device(rho_element, device=self.device)

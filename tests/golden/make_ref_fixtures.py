@@ -574,6 +574,12 @@ def main():
                                                   filter_radius=SC.constant(target_value=1.2)),
                                              load_frac=0.25))
     print(f"ref_loop_oc_defaults_10x5x4.npz ({time.perf_counter() - t:.1f} s)")
+    # the optional sensitivity filter (common_density.py:1102-1106)
+    t = time.perf_counter()
+    np.savez_compressed(os.path.join(HERE, "ref_loop_oc_sensfilter_12x6x6.npz"),
+                        **run_reference_loop(sk, "oc", (12, 6, 6), 5,
+                                             dict(bench_kw, sensitivity_filter=True)))
+    print(f"ref_loop_oc_sensfilter_12x6x6.npz ({time.perf_counter() - t:.1f} s)")
     t = time.perf_counter()
     np.savez_compressed(os.path.join(HERE, "ref_loop_logmoc_12x6x6.npz"),
                         **run_reference_loop(sk, "logmoc", (12, 6, 6), 6,

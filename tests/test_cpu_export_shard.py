@@ -107,6 +107,36 @@ def test_two_gloo_ranks_gather_design_results():
             assert got[i] == [float(i), float(r)]
 
 
+def _rank_subgroup(rank, world, port, out):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from sktopt_gb300.core import gather_design_results
+    grp = dist.new_group([1, 2])          # every rank creates it; rank 0 is not in it
+    if rank in (1, 2):
+        out[rank] = gather_design_results({rank * 10: [float(rank)]}, group=grp)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_gather_into_a_subgroup_without_global_rank_zero():
+    """A group of global ranks {1, 2}: the results land on global rank 1 (the
+    group's rank 0), not on global rank 0."""
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
+    out = mgr.dict()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_subgroup, args=(r, 3, port, out)) for r in range(3)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(120)
+        assert p.exitcode == 0
+    assert out[2] is None
+    assert out[1] == {10: [1.0], 20: [2.0]}
+
+
 def test_partition_more_ranks_than_designs():
     from sktopt_gb300.core import partition_designs
     parts = partition_designs([3.0, 1.0, 2.0], 5)

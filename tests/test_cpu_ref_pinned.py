@@ -175,7 +175,8 @@ def test_log_update_matches_reference(U):
     np.testing.assert_array_equal(up, U["llu_upper"])
 
 
-def _oracle_for(method, size, iters, load_frac=None, defaults=False, vf=0.3, radius=1.5):
+def _oracle_for(method, size, iters, load_frac=None, defaults=False, vf=0.3, radius=1.5,
+                sensfilter=False):
     m, pb, design, fixed, vol = problems.cantilever(*size, load_frac=load_frac)
     filt = problems.gaussian_filter_for(m, design, radius)
     if defaults:
@@ -184,7 +185,8 @@ def _oracle_for(method, size, iters, load_frac=None, defaults=False, vf=0.3, rad
     else:
         C = lambda v: oopt.Sched("Constant", v, v)  # noqa: E731
         cfg = oopt.OracleConfig(method=method, max_iters=iters, p=C(3.0), vol_frac=C(vf),
-                                move_limit=C(0.2), filter_radius=C(radius), E_min_coeff=1e-9)
+                                move_limit=C(0.2), filter_radius=C(radius), E_min_coeff=1e-9,
+                                sensitivity_filter=sensfilter)
     return oopt.OracleOptimizer(cfg, pb, filt, design, fixed, vol), design
 
 
@@ -193,6 +195,7 @@ def _oracle_for(method, size, iters, load_frac=None, defaults=False, vf=0.3, rad
     ("ref_loop_logmoc_12x6x6", "logmoc", (12, 6, 6), {"vf": 0.4}),
     ("ref_loop_oc_defaults_10x5x4", "oc", (10, 5, 4),
      {"defaults": True, "load_frac": 0.25, "radius": 1.2}),
+    ("ref_loop_oc_sensfilter_12x6x6", "oc", (12, 6, 6), {"sensfilter": True}),
 ])
 def test_oracle_loop_matches_reference_driver(name, method, size, kw):
     """The oracle loop against the reference's DensityMethod loop (OC / log-MOC,

@@ -30,6 +30,48 @@ def _logmoc_cfg(n_iter, precision, radius):
                          E_min_coeff=1e-9, solver_option="cg_pyamg", precision=precision)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_multi_load_tet_logmoc_helmholtz_matches_oracle(native_lib, precision):
+    """The multi-load unstructured configuration at small size against the
+    oracle loop (same mesh, Dirichlet nodes, 4 point-load cases and design
+    sets; NumPy/SciPy direct solves, the restated nodal Helmholtz filter and
+    log-MOC update): compliance per iteration 1e-8 (FP64 path) / 1e-6
+    (mixed), densities 1e-6 / 1e-5."""
+    from oracle import fem as ofem
+    from oracle import filters as ofilt
+    from oracle import mesh as omesh
+    from oracle import optim as oopt
+    from sktopt_gb300.core import LogMOC_Optimizer
+    from sktopt_gb300.mesh import toy_problem
+    n_iter, radius = 5, 3.2 * 0.25
+    tsk = toy_problem.multi_load_tet(8, 4, 4, 2.0, 1.0, 1.0, jitter=0.2, seed=3)
+    opt = LogMOC_Optimizer(_logmoc_cfg(n_iter, precision, radius), tsk, device=_dev())
+    opt.parameterize()
+    mesh = tsk.mesh
+    om = omesh.GridMesh(mesh.p, mesh.t, "tet", None, None, None)
+    dn = np.unique(np.asarray(tsk.dirichlet_nodes))
+    pb = ofem.ElasticProblem(om, dn, [np.asarray(f) for f in tsk.neumann_linear])
+    design = np.asarray(tsk.design_elements, dtype=np.int64)
+    fixed = np.setdiff1d(np.arange(mesh.nelements), design)
+    mask = np.zeros(mesh.nelements, bool)
+    mask[design] = True
+    vol = omesh.elements_volume(om)
+    np.testing.assert_allclose(vol, np.asarray(tsk.elements_volume), rtol=1e-14)
+    filt = ofilt.HelmholtzFilterNodal(om, vol, radius, mask)
+    C = lambda v: oopt.Sched("Constant", v, v)  # noqa: E731
+    ocfg = oopt.OracleConfig(method="logmoc", max_iters=n_iter, p=C(3.0), vol_frac=C(0.25),
+                             move_limit=C(0.2), filter_radius=C(radius), E_min_coeff=1e-9)
+    ref = oopt.OracleOptimizer(ocfg, pb, filt, design, fixed, vol)
+    ctol, rtol = (1e-8, 1e-6) if precision == "fp64" else (1e-6, 1e-5)
+    for k in range(n_iter):
+        opt.optimize_steps(1)
+        c_ref = ref.step()
+        c = opt.recorder.histories["compliance"][-1]
+        assert abs(c - c_ref) <= ctol * abs(c_ref), (k, c, c_ref)
+        np.testing.assert_allclose(opt._state.rho.cpu().numpy(), ref.rho, rtol=0, atol=rtol)
+        assert opt.lambda_v == pytest.approx(ref.lambda_v, rel=1e-6, abs=1e-12)
+
+
 def test_multi_load_tet_logmoc_helmholtz_mixed_vs_fp64(native_lib):
     """The multi-load unstructured configuration at small size: jittered P1
     tets on a 2x1x1 box, bottom clamped, 4 point-load cases solved as one

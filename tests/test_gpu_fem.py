@@ -131,25 +131,75 @@ def test_mixed_refined_compliance(native_lib):
 
 @pytest.mark.parametrize("ny", [10, 26, 31])   # node tiles 16, 27 and 32 nodes high
 def test_matrix_free_operator_matches_assembled(native_lib, ny):
-    """FP32 matrix-free operator of a uniform hex grid vs the assembled FP32
-    matrix (same enforced operator, FP32 rounding apart)."""
+    """FP32 matrix-free operator of a uniform hex grid -- the tensor-core
+    kernel (3xTF32) and the FP32-FMA kernel -- vs the assembled FP32 matrix
+    (same enforced operator, FP32 rounding apart)."""
+    _mf_vs_assembled((9, ny, 5), seed=11)
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 1), (2, 3, 1), (30, 14, 12), (61, 20, 9),
+                                   (7, 16, 33)])
+def test_matrix_free_tensor_core_operator_shapes(native_lib, shape):
+    """Ragged node columns (15 x 7 nodes per column) and z segments, a single
+    cell, and grids one column wide or tall."""
+    _mf_vs_assembled(shape, seed=sum(shape))
+
+
+def _mf_vs_assembled(shape, seed):
     import torch
     from sktopt_gb300.fea import composer
     from sktopt_gb300.fea.engine import FemEngine
     from sktopt_gb300.mesh import toy_problem
-    tsk = toy_problem.cantilever(9, ny, 5)
+    tsk = toy_problem.cantilever(*shape)
     Ke, _, _ = composer.element_matrices(tsk.mesh, 0.3)
-    rho = torch.from_numpy(_rho(tsk.mesh.nelements, 11, lo=1e-3)).to(_dev())
-    x = torch.from_numpy(np.random.default_rng(12).standard_normal((3 * tsk.mesh.nnodes, 1)))
+    rho = torch.from_numpy(_rho(tsk.mesh.nelements, seed, lo=1e-3)).to(_dev())
+    x = torch.from_numpy(np.random.default_rng(seed + 1).standard_normal(
+        (3 * tsk.mesh.nnodes, 1)))
     x32 = x.float().to(_dev())
-    out = []
-    for mf in (True, False):
-        eng = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True,
-                        matrix_free=mf)
-        eng.update(rho, 1.0, 1e-9, 3.0)
-        out.append(eng.spmv(x32, torch.float32).double().cpu().numpy())
-    ref = out[1]
-    np.testing.assert_allclose(out[0], ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+    sell = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True,
+                     matrix_free=False)
+    sell.update(rho, 1.0, 1e-9, 3.0)
+    ref = sell.spmv(x32, torch.float32).double().cpu().numpy()
+    eng = FemEngine(tsk.mesh, 3, Ke, tsk.dirichlet_mask, mixed=True, multigrid=True,
+                    matrix_free=True)
+    eng.update(rho, 1.0, 1e-9, 3.0)
+    outs = {}
+    for kind in (1, 0):
+        eng.set_mf_kernel(kind)
+        outs[kind] = eng.spmv(x32, torch.float32).double().cpu().numpy()
+        np.testing.assert_allclose(outs[kind], ref, rtol=0, atol=2e-6 * np.abs(ref).max())
+    assert eng.mf_error() == 0
+    # deterministic: a second product gives the same bits
+    eng.set_mf_kernel(1)
+    again = eng.spmv(x32, torch.float32).double().cpu().numpy()
+    assert np.array_equal(again, outs[1])
+
+
+def test_mixed_solve_tensor_core_operator_matches_fma(native_lib):
+    """The mixed solve (every operator mode: products, residuals b - Ax and
+    y - Ax inside the V-cycle, products with the p.q dot) with the tensor-core
+    operator against the FP32-FMA operator: same converged compliance, same
+    number of flexible-CG iterations to within two."""
+    import torch
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(40, 16, 14)
+    rho = torch.from_numpy(_rho(tsk.mesh.nelements, 21, lo=1e-3)).to(_dev())
+    res = {}
+    for kind in (1, 0):
+        fem = FEM_SimpLinearElasticity(tsk, 1e-9, solver_config=LinearSolverConfig(
+            solver="cg_pyamg", rtol=1e-8, precision="mixed"), device=_dev())
+        fem.build(rho, 3.0)
+        fem.engine.set_mf_kernel(kind)
+        U = torch.zeros((tsk.n_dof, 1), dtype=torch.float64, device=_dev())
+        comp = fem.solve_built(U)
+        st = fem.solve_history[-1]
+        res[kind] = (float(comp[0]), st.iters, U.cpu().numpy())
+        assert fem.engine.mf_error() == 0
+    (c1, it1, u1), (c0, it0, u0) = res[1], res[0]
+    assert abs(c1 - c0) <= 1e-9 * abs(c0)
+    assert abs(it1 - it0) <= 2, (it1, it0)
+    assert np.linalg.norm(u1 - u0) <= 1e-7 * np.linalg.norm(u0)
 
 
 def test_energy_and_sensitivity(native_lib):
@@ -197,3 +247,97 @@ def test_multi_load_block_rhs(native_lib):
         comp, st = eng.solve(Ft, U, method, 1, 1e-12 if method == 0 else 1e-9, 5000)
         assert st.status == 0, st
         np.testing.assert_allclose(comp, comp_ref, rtol=tol)
+
+
+@pytest.mark.parametrize("method", [0, 3, 4])
+def test_warm_start_with_zero_rhs_column(native_lib, method):
+    """A solve started from the caller's U (x0) whose second load case has a
+    zero right-hand side returns the zero vector in that column (the column
+    takes no iteration), and the first column as a cold solve does."""
+    import torch
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(12, 6, 6)
+    eng = _engine_for(tsk, mixed=method != 0)
+    rho = torch.from_numpy(_rho(tsk.mesh.nelements, 31, lo=0.01)).to(_dev())
+    eng.update(rho, 1.0, 1e-9, 3.0)
+    f = torch.from_numpy(np.asarray(tsk.neumann_linear[0])).to(_dev())
+    F = torch.stack([f, torch.zeros_like(f)], dim=1).contiguous()
+    U = torch.from_numpy(np.random.default_rng(5).standard_normal((tsk.n_dof, 2))).to(_dev())
+    comp, st = eng.solve(F, U, method, 1, 1e-10, 2000, 0.1, 50, x0=True)
+    assert st.status == 0
+    assert torch.count_nonzero(U[:, 1]).item() == 0
+    assert comp[1] == 0.0
+    U0 = torch.zeros((tsk.n_dof, 1), dtype=torch.float64, device=_dev())
+    comp0, _ = eng.solve(f[:, None].contiguous(), U0, method, 1, 1e-10, 2000, 0.1, 50)
+    assert abs(comp[0] - comp0[0]) <= 1e-9 * abs(comp0[0])
+
+
+def test_status_nonfinite_density(native_lib):
+    """A NaN density makes the solve end with TOPT_NONFINITE (a status code
+    on the host; nothing faults)."""
+    import torch
+    from sktopt_gb300 import _native as N
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(12, 6, 6)
+    for mixed, method in ((False, 0), (True, 4)):
+        eng = _engine_for(tsk, mixed=mixed)
+        r = _rho(tsk.mesh.nelements, 3, lo=0.01)
+        r[17] = np.nan
+        f = torch.from_numpy(np.asarray(tsk.neumann_linear[0])[:, None].copy()).to(_dev())
+        U = torch.zeros_like(f)
+        with pytest.raises(N.ToptError) as ei:
+            eng.update(torch.from_numpy(r).to(_dev()), 1.0, 1e-9, 3.0)
+            eng.solve(f, U, method, 1, 1e-8, 500, 0.1, 50)
+        assert ei.value.code == N.TOPT_NONFINITE
+
+
+def test_status_maxiter(native_lib):
+    """maxiter = 1 on a 12x6x6 solve to 1e-8 ends with TOPT_MAXITER (reported,
+    not raised, as the reference only logs CG non-convergence)."""
+    import torch
+    from sktopt_gb300 import _native as N
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(12, 6, 6)
+    for mixed, method in ((False, 0), (True, 4)):
+        eng = _engine_for(tsk, mixed=mixed)
+        eng.update(torch.from_numpy(_rho(tsk.mesh.nelements, 4, lo=0.01)).to(_dev()),
+                   1.0, 1e-9, 3.0)
+        f = torch.from_numpy(np.asarray(tsk.neumann_linear[0])[:, None].copy()).to(_dev())
+        U = torch.zeros_like(f)
+        comp, st = eng.solve(f, U, method, 1, 1e-8, 1, 0.1, 1)
+        assert st.status == N.TOPT_MAXITER, st
+        assert np.isfinite(comp[0])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_elastic_plugin_numpy_call_convention(native_lib, precision):
+    """FEM_SimpLinearElasticity at the reference's call convention
+    (solver_elastic.py:643-676): NumPy rho in, u_dofs (n_dof, L) NumPy
+    written in place, NumPy compliances and (n_elem, L) energies out; two
+    load cases on a 10x5x4 cantilever against the oracle's direct solves."""
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.cantilever(10, 5, 4)
+    f0 = np.asarray(tsk.neumann_linear[0])
+    f1 = np.zeros_like(f0)
+    ijk = tsk.mesh.node_ijk
+    top = np.nonzero((ijk[0] == 10) & (ijk[2] == 4))[0]
+    f1[3 * top + 1] = 0.5 / top.size
+    tsk.neumann_linear = [f0, f1]
+    fem = FEM_SimpLinearElasticity(tsk, 1e-9, solver_config=LinearSolverConfig(
+        solver="spsolve", precision=precision), device=_dev())
+    rho = _rho(tsk.mesh.nelements, 41, lo=0.05)
+    u_dofs = np.zeros((tsk.n_dof, 2))
+    comp = fem.objectives_multi_load(rho, 3.0, u_dofs)
+    assert isinstance(comp, np.ndarray) and comp.shape == (2,)
+    en = fem.energy_multi_load(rho, 3.0, u_dofs)
+    assert isinstance(en, np.ndarray) and en.shape == (tsk.mesh.nelements, 2)
+    m, pb, *_ = problems.cantilever(10, 5, 4)
+    pb.forces = [f0, f1]
+    comp_ref, U_ref = pb.objectives(rho, 3.0, 1e-9, "spsolve")
+    en_ref = pb.energy(rho, 3.0, 1e-9, U_ref)
+    tol = 1e-10 if precision == "fp64" else 1e-6
+    np.testing.assert_allclose(comp, comp_ref, rtol=tol)
+    np.testing.assert_allclose(u_dofs, U_ref, rtol=0, atol=tol * np.abs(U_ref).max())
+    assert np.linalg.norm(en - en_ref) <= (1e-9 if precision == "fp64" else 1e-5) * \
+        np.linalg.norm(en_ref)

@@ -111,6 +111,8 @@ def _run_loop(method, size, n_iter, fixture, precision, load_frac=None, **cfg_ov
     ("ref_loop_oc_12x6x6.npz", "oc", (12, 6, 6), "mixed", {}),
     ("ref_loop_logmoc_12x6x6.npz", "logmoc", (12, 6, 6), "fp64", {"vf": 0.4}),
     ("ref_loop_oc_defaults_10x5x4.npz", "oc", (10, 5, 4), "fp64", {"defaults": True}),
+    ("ref_loop_oc_sensfilter_12x6x6.npz", "oc", (12, 6, 6), "fp64",
+     {"sensitivity_filter": True}),
 ])
 def test_loop_matches_reference_driver(native_lib, fixture, method, size, precision, kw):
     """Whole loops against the reference driver: compliance per iteration
@@ -129,6 +131,8 @@ def test_loop_matches_reference_driver(native_lib, fixture, method, size, precis
         load_frac = 0.25
     if "vf" in kw:
         over["vol_frac"] = S.constant(target_value=kw["vf"])
+    if kw.get("sensitivity_filter"):
+        over["sensitivity_filter"] = True
     R = _load(fixture)
     n = int(R["iters"])
     opt, R, snaps = _run_loop(method, size, n, fixture, precision, load_frac, **over)

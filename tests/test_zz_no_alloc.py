@@ -40,6 +40,20 @@ def test_noalloc_dot_matches_allocating_dot_twice(native_lib):
         assert abs(ref - float(torch.dot(x, y).item())) <= 1e-12 * scale
 
 
+def test_noalloc_dot_at_the_scratch_boundaries(native_lib):
+    """One full chunk (65,536 elements, one partial sum), one element past
+    4,095 full chunks (the last partial-sum slot holds a single product) and
+    the maximum size (every slot used, the last chunk full), twice each; with
+    x = y = 1 every partial is an integer, so the sum is exact."""
+    import torch
+    for n in (65_536, 4095 * 65_536 + 1, 4096 * 65_536):
+        x = torch.ones(n, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            assert _dot(native_lib, "topt_reduce_dot_noalloc", x, x) == float(n)
+        del x
+        torch.cuda.empty_cache()
+
+
 def test_noalloc_dot_rejects_sizes_beyond_its_scratch(native_lib):
     import torch
     x = torch.zeros(8, dtype=torch.float64, device="cuda")
