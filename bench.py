@@ -498,8 +498,9 @@ def run_reference(args):
 
 def probe_spmv(size):
     """Profiling target: assemble the mixed engine for a cantilever of `size`
-    and run the level-0 operator twice in FP32 (matrix-free, NVTX range
-    "spmv32") and twice in FP64 (assembled SELL, range "spmv64"), then the
+    and run the level-0 operator twice in FP32 on the tensor cores (k_mf_tc,
+    NVTX range "spmv32"), twice with the FP32-FMA kernel (k_mf_tile, range
+    "spmv32fma") and twice in FP64 (assembled SELL, range "spmv64"), then the
     FP32 assembled SELL product of an engine without the matrix-free operator
     twice (range "spmv32sell", the kernel of the coarse levels)."""
     import numpy as np
@@ -516,7 +517,10 @@ def probe_spmv(size):
     x32 = torch.rand((eng.n_dof, 1), dtype=torch.float32, device=dev)
     x64 = x32.double()
     torch.cuda.synchronize()
-    for name, x, dt in (("spmv32", x32, torch.float32), ("spmv64", x64, torch.float64)):
+    for name, x, dt, kind in (("spmv32", x32, torch.float32, 1),
+                              ("spmv32fma", x32, torch.float32, 0),
+                              ("spmv64", x64, torch.float64, 1)):
+        eng.set_mf_kernel(kind)
         torch.cuda.nvtx.range_push(name)
         for _ in range(2):
             eng.spmv(x, dt)

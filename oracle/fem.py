@@ -220,6 +220,12 @@ def solve(Ke, Fe, solver="spsolve", rtol=1e-8, maxiter=None):
             lu = spla.splu(Ke.tocsc())
             return lu.solve(Fe)
         return spla.spsolve(Ke.tocsc(), Fe)
+    if solver == "spsolve_mmd":
+        # the same direct solve with SuperLU's minimum-degree ordering of
+        # A^T + A: less fill on these symmetric 3-D systems, several times
+        # faster at 60x20x20, the same solution to rounding
+        lu = spla.splu(Ke.tocsc(), permc_spec="MMD_AT_PLUS_A")
+        return lu.solve(Fe)
     if solver == "cg_jacobi":
         Minv = 1.0 / Ke.diagonal()
         M = spla.LinearOperator(Ke.shape, matvec=lambda x: Minv * x)

@@ -45,8 +45,9 @@ Run from the repository root (the reference tree must be present):
 
     python tests/golden/make_ref_fixtures.py [--c1]
 
-``--c1`` also runs the 60x20x20 cantilever for 30 iterations (a few
-minutes).  Outputs: tests/golden/ref_*.npz.
+``--c1`` also runs the 60x20x20 cantilever for 30 iterations (about half
+an hour: one direct solve of 80,703 DOFs per iteration).  Outputs:
+tests/golden/ref_*.npz and ref_config_defaults.json.
 """
 from __future__ import annotations
 
@@ -392,7 +393,8 @@ def _silence(opt):
     opt.schedulers.export = lambda *a, **k: None
 
 
-def run_reference_loop(sk, method, size, iters, cfg_kw, snap_iters=(), load_frac=None):
+def run_reference_loop(sk, method, size, iters, cfg_kw, snap_iters=(), load_frac=None,
+                       solver="spsolve"):
     """The reference driver (common_density.py:966-1243) on the cantilever of
     `size` for `iters` iterations.  Returns per-iteration histories and the
     density after each iteration in `snap_iters`."""
@@ -411,7 +413,7 @@ def run_reference_loop(sk, method, size, iters, cfg_kw, snap_iters=(), load_frac
         cfg.record_times = iters
         cfg.dst_path = d
         opt = cls(cfg, tsk)
-        fem = OracleFEM(pb, 1.0, cfg.E_min_coeff)
+        fem = OracleFEM(pb, 1.0, cfg.E_min_coeff, solver=solver)
         opt.fem = fem
         opt.parameterize()
         opt.filter = CachedSpacialFilter(opt.filter)
@@ -589,7 +591,11 @@ def main():
     print(f"ref_loop_logmoc_12x6x6.npz ({time.perf_counter() - t:.1f} s)")
     if args.c1:
         t = time.perf_counter()
-        res = run_reference_loop(sk, "oc", (60, 20, 20), 30, bench_kw, snap_iters=(10,))
+        # direct solves with the minimum-degree ordering (oracle solver
+        # "spsolve_mmd"): the reference's default COLAMD ordering takes
+        # minutes per solve at this size
+        res = run_reference_loop(sk, "oc", (60, 20, 20), 30, bench_kw, snap_iters=(10,),
+                                 solver="spsolve_mmd")
         keep = {k: v for k, v in res.items() if k not in ("rho_final", "rho_projected_final",
                                                          "design",
                                                          "dirichlet_neumann_elements")}

@@ -137,11 +137,11 @@ def test_matrix_free_operator_matches_assembled(native_lib, ny):
     _mf_vs_assembled((9, ny, 5), seed=11)
 
 
-@pytest.mark.parametrize("shape", [(1, 1, 1), (2, 3, 1), (30, 14, 12), (61, 20, 9),
+@pytest.mark.parametrize("shape", [(3, 1, 1), (2, 3, 1), (30, 14, 12), (61, 20, 9),
                                    (7, 16, 33)])
 def test_matrix_free_tensor_core_operator_shapes(native_lib, shape):
-    """Ragged node columns (15 x 7 nodes per column) and z segments, a single
-    cell, and grids one column wide or tall."""
+    """Ragged node columns (15 x 7 nodes per column) and z segments, a grid
+    one cell thick, and grids one column wide or tall."""
     _mf_vs_assembled(shape, seed=sum(shape))
 
 
