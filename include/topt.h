@@ -122,8 +122,8 @@ int topt_fem_set_interpolation(topt_fem* h, int32_t kind);
 int topt_fem_set_element_extra(topt_fem* h, const double* extra);
 
 /* Kernel of the matrix-free FP32 level-0 operator (handles created with
- * mf_level0 on a uniform hex grid): 1 = tensor cores (tcgen05, TF32 with the
- * 3xTF32 split, FP32-accurate; the default), 0 = FP32 FMA tiles.  Both compute
+ * mf_level0 on a uniform hex grid): 0 = FP32 FMA tiles (the default),
+ * 1 = tensor cores (tcgen05, TF32 with the 3xTF32 split, FP32-accurate).  Both compute
  * the same operator (the element products of composer.py:53-101 on one unit
  * matrix, enforce as identity rows); they differ by rounding only.
  * mf_error (may be NULL) receives 1 if a tensor-core launch gave up on one

@@ -121,8 +121,9 @@ struct topt_fem {
   topt::MfGrid mfg{};
   int mf_ty = 32;                      // y extent of the operator's node tiles
   topt::K0f k0{};                      // FP32 unit matrix (by-value kernel parameter)
-  // tensor-core operator (k_mf_tc): 0 = FP32-FMA tiles (k_mf_tile), 1 = tcgen05
-  int mf_kernel = 1;
+  // fine-level operator kernel: 0 = FP32-FMA tiles (k_mf_tile, the default:
+  // measured faster), 1 = tensor cores (k_mf_tc)
+  int mf_kernel = 0;
   topt::MfTcGrid mftc{};
   topt::DevBuf k0img;                  // K0 hi / lo in the MMA operand layout
   topt::DevBuf mf_err;                 // set by k_mf_tc if an mbarrier wait times out
@@ -384,20 +385,24 @@ static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y,
 }
 
 // Tensor-core variant: persistent, two CTAs per SM over (column, z segment)
-// work items.
+// work items; node planes and the drainers' per-layer data in rings of
+// kMfTcNpl and kMfTcNel, suspending mbarrier waits.
+constexpr int kMfTcNpl = 3, kMfTcNel = 3, kMfTcWait = 1;
+
 template <int MODE, bool DOT, bool COLMASK>
 static int launch_mf_tc(topt_fem* h, const float* x, const float* b, float* y, int slot) {
+  constexpr uint32_t smem = mftc::smem_bytes(kMfTcNpl, kMfTcNel);
+  auto kern = k_mf_tc<MODE, DOT, COLMASK, kMfTcNpl, kMfTcNel, kMfTcWait>;
   static bool attr_set = false;   // per instantiation, process-wide
   if (!attr_set) {
-    TOPT_CUDA(cudaFuncSetAttribute(k_mf_tc<MODE, DOT, COLMASK>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)mftc::SMEM));
+    TOPT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     attr_set = true;
   }
   const MfTcGrid& G = h->mftc;
   const int64_t items = (int64_t)G.ncy * G.ncx * G.nseg;
   const int grid = (int)std::min<int64_t>(items, (int64_t)h->sm * 2);
-  k_mf_tc<MODE, DOT, COLMASK><<<grid, mftc::THREADS, mftc::SMEM, h->stream>>>(
+  kern<<<grid, mftc::THREADS, smem, h->stream>>>(
       G, h->k0img.as<float>(), h->coef32.as<float>(), h->nmask32.as<uint32_t>(), x, b, y,
       h->red.partials.as<double>(), h->red.ctr(slot), h->red.res(slot),
       h->mf_err.as<int>());

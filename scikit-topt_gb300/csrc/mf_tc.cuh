@@ -14,20 +14,24 @@
 // scaled by coef_m and stored to shared memory; each node sums the rows of
 // its 8 cells (two consecutive cell layers) in a fixed order, so the result
 // is deterministic.  Cells on the column's border are computed by both
-// neighbouring columns (16 x 8 cells for 15 x 7 nodes).
+// neighbouring columns (16 x 8 cells for 15 x 7 nodes); cells outside the
+// grid have coefficient 0.
 //
-// Warp roles (256 threads), so that consecutive layers overlap:
-//   builders (warps 0-3): stage node planes (cp.async), build the A tile of
-//     layer L into A[L % 2] once the MMAs of layer L-2 have released it, and
-//     (thread 0) issue layer L's MMAs into TMEM buffer L % 2 once the
-//     drainers have emptied it, committing them to mbarrier full[L % 2];
+// Warp roles (288 threads), so that consecutive layers overlap:
+//   builders (warps 0-3): stage node planes (cp.async), split each node's x
+//     once into TF32 hi / lo parts, and build the A tile of layer L into
+//     A[L % 2] once the MMAs of layer L-2 have released it (mbarrier
+//     full[L % 2]); then arrive on mbarrier ready[L % 2];
+//   issuer (warp 8, one lane): waits ready[L % 2] and, for the TMEM buffer,
+//     empty[L % 2] (layer L-2 drained), issues layer L's 9 MMAs and commits
+//     them to full[L % 2];
 //   drainers (warps 4-7, lanes 0-127 of tensor memory): wait full[L % 2],
-//     load the accumulators, release the TMEM buffer (mbarrier empty[L % 2]),
-//     scale by the cell coefficients, store Y[L % 2] and produce the node
-//     plane of layer L from Y[L % 2] and Y[(L-1) % 2].
-// Each role synchronises internally with its own named barrier.
+//     load the accumulators, release the TMEM buffer (empty[L % 2]), scale
+//     by the cell coefficients, store Y[L % 2] and produce the node plane of
+//     layer L from Y[L % 2] and Y[(L-1) % 2].
+// Builders and drainers each synchronise internally with a named barrier.
 //
-// Every wait is bounded: on a timeout the CTA sets an abort flag that both
+// Every wait is bounded: on a timeout the CTA sets an abort flag that all
 // roles poll, stops, lets in-flight MMAs drain, writes a NaN into y (the
 // solvers then stop with a non-finite status), records the error and frees
 // its tensor memory.
@@ -41,18 +45,24 @@ namespace mftc {
 constexpr int CY = 16, CX = 8;              // cells per layer tile
 constexpr int NY = CY - 1, NX = CX - 1;     // output nodes per plane
 constexpr int HY = CY + 1, HX = CX + 1;     // halo nodes per plane
+constexpr int NHALO = HY * HX;              // 153
 constexpr int M = CY * CX;                  // 128 = MMA rows
 constexpr int NPN = NY * NX;                // 105 output nodes per plane
-constexpr int GROUP = 128;                  // threads per role
-constexpr int THREADS = 2 * GROUP;
+constexpr int GROUP = 128;                  // threads per builder / drainer role
+constexpr int THREADS = 2 * GROUP + 32;     // + the issuing warp
 constexpr uint32_t SBO_A = 12 * 128;        // 48 K columns = 12 core matrices
 constexpr uint32_t SBO_B = 6 * 128;         // 24 K columns
-constexpr int YS = 36;                      // floats per Y row (8 x float4 + pad)
-constexpr int NPLANE = 3;                   // builders' node-plane ring
+// Y rows: 8 float4 (one per local node, .w unused), the float4 of local
+// node la of row m stored at position la ^ (m & 7), so that eight
+// consecutive rows touch eight different 16-byte bank groups
+constexpr int YS = 32;
 constexpr uint32_t A_BYTES = M * 48 * 4;    // 24576
 constexpr uint32_t B_BYTES = 32 * 24 * 4;   // 3072 per split part
-constexpr uint32_t Y_BYTES = M * YS * 4;    // 18432
-constexpr uint32_t P_BYTES = HY * HX * 16;  // 2448 (float4 per halo node)
+constexpr uint32_t Y_BYTES = M * YS * 4;    // 16384
+// node planes: per halo node the TF32 hi (x, y, z, 0) and lo parts
+// (x, y, z, 0) as two float4; cp.async lands the raw values (x, y, z and
+// the fixed bits) in the hi slot
+constexpr uint32_t P_BYTES = NHALO * 32;    // 4896
 // drainers' per-layer slot: coefficients (128), own node x + flags (105 x
 // float4), b or y of the own node (105 x 3)
 constexpr uint32_t E_COEF = 0, E_SELF = M * 4, E_SRC = E_SELF + NPN * 16;
@@ -61,9 +71,15 @@ constexpr uint32_t OFF_A = 0;
 constexpr uint32_t OFF_B = OFF_A + 2 * A_BYTES;
 constexpr uint32_t OFF_Y = OFF_B + 2 * B_BYTES;
 constexpr uint32_t OFF_P = OFF_Y + 2 * Y_BYTES;
-constexpr uint32_t OFF_E = OFF_P + NPLANE * P_BYTES;
-constexpr uint32_t OFF_BAR = OFF_E + 2 * E_BYTES;   // full[2], empty[2], tmem slot, abort
-constexpr uint32_t SMEM = OFF_BAR + 64;
+// node planes (NPL) and drainer slots (NEL) in rings: plane c + NPL - 1 and
+// the drainers' data of layer c + NEL - 1 are loading while layer c is built
+__host__ __device__ constexpr uint32_t off_e(int NPL) { return OFF_P + NPL * P_BYTES; }
+__host__ __device__ constexpr uint32_t off_bar(int NPL, int NEL) {
+  return off_e(NPL) + NEL * E_BYTES;   // full, empty, ready [2], tmem slot, abort flag
+}
+__host__ __device__ constexpr uint32_t smem_bytes(int NPL, int NEL) {
+  return off_bar(NPL, NEL) + 64;
+}
 constexpr uint32_t TMEM_COLS = 64;
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 // image of K0 hi / lo in the B layout, built on the host (2 x 768 floats)
@@ -81,6 +97,10 @@ __device__ __forceinline__ void mftc_cp4(void* s, const void* gp, bool in) {
                "r"(in ? 4 : 0));
 }
 __device__ __forceinline__ void mftc_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void mftc_wait_groups() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
 
 // Named barrier of one role (id 1: builders, 2: drainers), returning the OR
 // of `fail` over the role.
@@ -99,20 +119,34 @@ __device__ __forceinline__ void mftc_group_sync(int id) {
 }
 
 // Bounded wait on an mbarrier phase that also gives up when the CTA's abort
-// flag is set.
+// flag is set.  WAITK 0 polls with mbarrier.test_wait (never blocks);
+// WAITK 1 uses mbarrier.try_wait, which suspends the warp in hardware until
+// the phase completes or a system-dependent time limit passes, so waiting
+// warps leave the issue slots to working ones.  Both are bounded by the
+// poll count.
+template <int WAITK>
 __device__ __forceinline__ bool mftc_wait(uint64_t* bar, uint32_t parity,
                                           const volatile int* abort_f) {
   const uint32_t a = tc::smem_u32(bar);
-  for (uint32_t i = 0; i < mftc::WAIT_LIMIT; ++i) {
+  const uint32_t limit = WAITK == 0 ? mftc::WAIT_LIMIT : (mftc::WAIT_LIMIT >> 8);
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
-    asm volatile(
-        "{\n .reg .pred P1;\n mbarrier.test_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
-        " selp.b32 %0, 1, 0, P1;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
+    if (WAITK == 0)
+      asm volatile(
+          "{\n .reg .pred P1;\n mbarrier.test_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+          " selp.b32 %0, 1, 0, P1;\n}\n"
+          : "=r"(done)
+          : "r"(a), "r"(parity)
+          : "memory");
+    else
+      asm volatile(
+          "{\n .reg .pred P1;\n mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n"
+          " selp.b32 %0, 1, 0, P1;\n}\n"
+          : "=r"(done)
+          : "r"(a), "r"(parity)
+          : "memory");
     if (done) return true;
-    if ((i & 255) == 255 && *abort_f) return false;
+    if ((WAITK == 1 || (i & 255) == 255) && *abort_f) return false;
   }
   return false;
 }
@@ -122,24 +156,52 @@ __device__ __forceinline__ void mftc_arrive(uint64_t* bar) {
                : "memory");
 }
 
-// Node plane z of the column's halo (builders): x in .xyz, the fixed-DOF
-// bits in .w, zeros outside the grid.
+// Per-phase time stamps for experiments (no-op unless defined before this
+// header is included).
+#ifndef MFTC_MARK
+#define MFTC_MARK(role, ev)
+#endif
+
+// Node plane z of the column's halo (builders): x and the fixed-DOF bits
+// into the hi slot of each halo node, zeros outside the grid.
 __device__ __forceinline__ void mftc_stage_plane(float* P, int z, int y0, int x0, int ny1,
                                                  int nx1, int nz1, int t,
                                                  const float* __restrict__ x,
                                                  const uint32_t* __restrict__ m32) {
   using namespace mftc;
   const bool zin = z >= 0 && z < nz1;
-  for (int q = t; q < HY * HX; q += GROUP) {
+  for (int q = t; q < NHALO; q += GROUP) {
     const int hy = q % HY, hx = q / HY;
     const int gy = y0 - 1 + hy, gx = x0 - 1 + hx;
     const bool in = zin && gy >= 0 && gy < ny1 && gx >= 0 && gx < nx1;
     const int64_t n = in ? (int64_t)gy + (int64_t)ny1 * (gx + (int64_t)nx1 * z) : 0;
-    float* d = P + q * 4;
+    float* d = P + q * 8;
     mftc_cp4(d + 0, x + n * 3 + 0, in);
     mftc_cp4(d + 1, x + n * 3 + 1, in);
     mftc_cp4(d + 2, x + n * 3 + 2, in);
     mftc_cp4(d + 3, m32 + n, in);
+  }
+}
+
+// Split a landed plane in place: hi = tf32(x), lo = tf32(x - hi), masked
+// components zeroed first (COLMASK).  Each thread rewrites the halo nodes it
+// staged itself.
+template <bool COLMASK>
+__device__ __forceinline__ void mftc_split_plane(float* P, int t) {
+  using namespace mftc;
+  for (int q = t; q < NHALO; q += GROUP) {
+    float4* d = reinterpret_cast<float4*>(P + q * 8);
+    const float4 v = d[0];
+    float a0 = v.x, a1 = v.y, a2 = v.z;
+    if (COLMASK) {
+      const int mk = __float_as_int(v.w);
+      a0 = (mk & 1) ? 0.f : a0;
+      a1 = (mk & 2) ? 0.f : a1;
+      a2 = (mk & 4) ? 0.f : a2;
+    }
+    const float h0 = tc::to_tf32(a0), h1 = tc::to_tf32(a1), h2 = tc::to_tf32(a2);
+    d[0] = make_float4(h0, h1, h2, 0.f);
+    d[1] = make_float4(tc::to_tf32(a0 - h0), tc::to_tf32(a1 - h1), tc::to_tf32(a2 - h2), 0.f);
   }
 }
 
@@ -179,24 +241,40 @@ __device__ __forceinline__ void mftc_stage_own(unsigned char* S, int c, int y0, 
   }
 }
 
-template <int MODE, bool DOT, bool COLMASK>
-__global__ void __launch_bounds__(mftc::THREADS, 2)
+// The work item sequence every role walks: (column origin, z range).
+struct MftcItem {
+  int y0, x0, z0, z1;
+};
+__device__ __forceinline__ MftcItem mftc_item(const MfTcGrid& G, int item, int nz1) {
+  using namespace mftc;
+  const int col = item % (G.ncy * G.ncx), seg = item / (G.ncy * G.ncx);
+  MftcItem it;
+  it.y0 = (col % G.ncy) * NY;
+  it.x0 = (col / G.ncy) * NX;
+  it.z0 = seg * G.zs;
+  it.z1 = min(nz1, it.z0 + G.zs);
+  return it;
+}
+
+// 112 registers: two CTAs of 288 threads fit the register file.
+template <int MODE, bool DOT, bool COLMASK, int NPL, int NEL, int WAITK>
+__global__ void __maxnreg__(112)
 k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ coef,
         const uint32_t* __restrict__ m32, const float* __restrict__ x,
         const float* __restrict__ b, float* __restrict__ y, double* partials,
         unsigned* counter, double* dot_out, int* err) {
   TOPT_KERNEL_COUNT();
   using namespace mftc;
+  static_assert(NPL >= 3 && NEL >= 2, "rings too short");
   extern __shared__ __align__(1024) unsigned char mftc_smem[];
   unsigned char* smem = mftc_smem;
   float* Bs = reinterpret_cast<float*>(smem + OFF_B);
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + OFF_BAR);
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + off_bar(NPL, NEL));
   uint64_t* empty = full + 2;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + OFF_BAR + 32);
-  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + OFF_BAR + 48);
+  uint64_t* ready = full + 4;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + off_bar(NPL, NEL) + 48);
+  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + off_bar(NPL, NEL) + 56);
   const int tid = threadIdx.x, warp = tid >> 5;
-  const bool builder = tid < GROUP;
-  const int t = builder ? tid : tid - GROUP;
   const MfGrid& g = G.g;
   const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
   const float* bsrc = MODE == 1 ? b : y;
@@ -209,6 +287,8 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
     tc::mbar_init(&full[1], 1);
     tc::mbar_init(&empty[0], GROUP);
     tc::mbar_init(&empty[1], GROUP);
+    tc::mbar_init(&ready[0], GROUP);
+    tc::mbar_init(&ready[1], GROUP);
     *abort_f = 0;
     tc::mbar_init_fence();
   }
@@ -218,131 +298,115 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
-  bool fail = false;           // uniform within the role after each role sync
+  bool fail = false;           // uniform within a role after each role sync
   float tacc = 0.0f;
-  uint32_t L = 0;              // running layer count (same sequence in both roles)
+  uint32_t L = 0;              // running layer count (the same sequence in every role)
   const int nitems = G.ncy * G.ncx * G.nseg;
 
-  if (builder) {
-    const uint32_t idesc = tc::idesc_tf32(M, 32);
+  if (warp < 4) {
+    // ------------------------------------------------------------ builders
+    const int t = tid;
+    auto plane = [&](int z) {
+      return reinterpret_cast<float*>(smem + OFF_P + ((z + NPL) % NPL) * P_BYTES);
+    };
     for (int item = blockIdx.x; item < nitems && !fail; item += gridDim.x) {
-      const int col = item % (G.ncy * G.ncx), seg = item / (G.ncy * G.ncx);
-      const int y0 = (col % G.ncy) * NY, x0 = (col / G.ncy) * NX;
-      const int z0 = seg * G.zs, z1 = min(nz1, z0 + G.zs);
-      auto plane = [&](int z) {
-        return reinterpret_cast<float*>(smem + OFF_P + ((z + NPLANE) % NPLANE) * P_BYTES);
-      };
-      mftc_stage_plane(plane(z0 - 1), z0 - 1, y0, x0, ny1, nx1, nz1, t, x, m32);
-      mftc_commit();
-      mftc_stage_plane(plane(z0), z0, y0, x0, ny1, nx1, nz1, t, x, m32);
-      mftc_commit();
-      for (int c = z0 - 1; c < z1; ++c, ++L) {
-        if (c + 2 <= z1) mftc_stage_plane(plane(c + 2), c + 2, y0, x0, ny1, nx1, nz1, t, x, m32);
+      const MftcItem it = mftc_item(G, item, nz1);
+      // planes z0-1 .. z0+NPL-3 in flight before the first layer
+      for (int z = it.z0 - 1; z <= it.z0 + NPL - 3; ++z) {
+        if (z <= it.z1) mftc_stage_plane(plane(z), z, it.y0, it.x0, ny1, nx1, nz1, t, x, m32);
         mftc_commit();
-        asm volatile("cp.async.wait_group 1;\n" ::);
+      }
+      for (int c = it.z0 - 1; c < it.z1; ++c, ++L) {
+        MFTC_MARK(0, 0);
+        mftc_wait_groups<NPL - 3>();          // planes c and c + 1 have landed
+        // the split below rewrites only this thread's own staged nodes; the
+        // barrier makes every builder past layer c-1 before plane c-1's slot
+        // is refilled
+        if (mftc_group_sync_or(1, fail)) { fail = true; break; }
+        const int zp = c + NPL - 1;
+        if (zp <= it.z1)
+          mftc_stage_plane(plane(zp), zp, it.y0, it.x0, ny1, nx1, nz1, t, x, m32);
+        mftc_commit();
+        if (c == it.z0 - 1) mftc_split_plane<COLMASK>(plane(c), t);
+        mftc_split_plane<COLMASK>(plane(c + 1), t);
         // A[L % 2] is free once the MMAs of layer L-2 have completed
-        const bool ok = L < 2 || mftc_wait(&full[L & 1], ((L - 2) >> 1) & 1u, abort_f);
-        if (mftc_group_sync_or(1, fail || !ok)) { fail = true; break; }
+        const bool ok = L < 2 || mftc_wait<WAITK>(&full[L & 1], ((L - 2) >> 1) & 1u, abort_f);
+        if (mftc_group_sync_or(1, !ok)) { fail = true; break; }
+        MFTC_MARK(0, 1);
         // A tile of cell layer c: row t = cell (t % 16, t / 16)
         {
           const int rcy = t % CY, rcx = t / CY;
-          const int cy = y0 - 1 + rcy, cx = x0 - 1 + rcx;
-          const bool cin = c >= 0 && c < g.nz && cy >= 0 && cy < g.ny && cx >= 0 && cx < g.nx;
           const float4* P0 = reinterpret_cast<const float4*>(plane(c));
           const float4* P1 = reinterpret_cast<const float4*>(plane(c + 1));
-          float xv[24];
+          float xh[24], xl[24];
 #pragma unroll
           for (int lb = 0; lb < 8; ++lb) {
             const float4* P = hoff(lb, 2) ? P1 : P0;
-            const float4 v = P[(rcx + hoff(lb, 0)) * HY + rcy + hoff(lb, 1)];
-            float a0 = v.x, a1 = v.y, a2 = v.z;
-            if (COLMASK) {
-              const int mk = __float_as_int(v.w);
-              a0 = (mk & 1) ? 0.f : a0;
-              a1 = (mk & 2) ? 0.f : a1;
-              a2 = (mk & 4) ? 0.f : a2;
-            }
-            xv[3 * lb + 0] = cin ? a0 : 0.f;
-            xv[3 * lb + 1] = cin ? a1 : 0.f;
-            xv[3 * lb + 2] = cin ? a2 : 0.f;
+            const int q = (rcx + hoff(lb, 0)) * HY + rcy + hoff(lb, 1);
+            const float4 h = P[2 * q], l = P[2 * q + 1];
+            xh[3 * lb + 0] = h.x;
+            xh[3 * lb + 1] = h.y;
+            xh[3 * lb + 2] = h.z;
+            xl[3 * lb + 0] = l.x;
+            xl[3 * lb + 1] = l.y;
+            xl[3 * lb + 2] = l.z;
           }
           unsigned char* A = smem + OFF_A + (L & 1) * A_BYTES;
 #pragma unroll
           for (int q = 0; q < 6; ++q) {
-            float4 hi, lo;
-            hi.x = tc::to_tf32(xv[4 * q + 0]);
-            hi.y = tc::to_tf32(xv[4 * q + 1]);
-            hi.z = tc::to_tf32(xv[4 * q + 2]);
-            hi.w = tc::to_tf32(xv[4 * q + 3]);
-            lo.x = tc::to_tf32(xv[4 * q + 0] - hi.x);
-            lo.y = tc::to_tf32(xv[4 * q + 1] - hi.y);
-            lo.z = tc::to_tf32(xv[4 * q + 2] - hi.z);
-            lo.w = tc::to_tf32(xv[4 * q + 3] - hi.w);
-            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 4 * q, SBO_A)) = hi;
-            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 24 + 4 * q, SBO_A)) = lo;
+            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 4 * q, SBO_A)) =
+                make_float4(xh[4 * q], xh[4 * q + 1], xh[4 * q + 2], xh[4 * q + 3]);
+            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 24 + 4 * q, SBO_A)) =
+                make_float4(xl[4 * q], xl[4 * q + 1], xl[4 * q + 2], xl[4 * q + 3]);
           }
           tc::fence_async_smem();
         }
-        mftc_group_sync(1);
-        if (t == 0) {
-          // TMEM buffer L % 2 is free once the drainers have read layer L-2
-          const bool ok0 = L < 2 || mftc_wait(&empty[L & 1], ((L - 2) >> 1) & 1u, abort_f);
-          if (ok0) {
-            tc::fence_after_sync();
-            const uint32_t a0 = tc::smem_u32(smem + OFF_A + (L & 1) * A_BYTES);
-            const uint32_t bh = tc::smem_u32(Bs), bl = bh + B_BYTES;
-            const uint32_t d = tmem + (L & 1) * 32u;
-#pragma unroll
-            for (int s = 0; s < 6; ++s)
-              tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A),
-                           tc::sdesc(bh + 256u * (s % 3), 128u, SBO_B), idesc, s > 0 ? 1u : 0u);
-#pragma unroll
-            for (int s = 0; s < 3; ++s)
-              tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A),
-                           tc::sdesc(bl + 256u * s, 128u, SBO_B), idesc, 1u);
-            tc::mma_commit(&full[L & 1]);
-          } else {
-            *const_cast<int*>(abort_f) = 1;
-            fail = true;
-          }
-        }
+        mftc_arrive(&ready[L & 1]);
+        MFTC_MARK(0, 2);
       }
-      asm volatile("cp.async.wait_group 0;\n" ::);
+      mftc_wait_groups<0>();
     }
-  } else {
-    const int e = t;
+  } else if (warp < 8) {
+    // ------------------------------------------------------------ drainers
+    const int e = tid - GROUP;
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
     for (int item = blockIdx.x; item < nitems && !fail; item += gridDim.x) {
-      const int col = item % (G.ncy * G.ncx), seg = item / (G.ncy * G.ncx);
-      const int y0 = (col % G.ncy) * NY, x0 = (col / G.ncy) * NX;
-      const int z0 = seg * G.zs, z1 = min(nz1, z0 + G.zs);
-      mftc_stage_own<MODE>(smem + OFF_E, z0 - 1, y0, x0, g, e, coef, x, m32, bsrc);
-      mftc_commit();
-      int i = 0;
-      for (int c = z0 - 1; c < z1; ++c, ++L, ++i) {
-        unsigned char* S = smem + OFF_E + (i & 1) * E_BYTES;
-        mftc_stage_own<MODE>(smem + OFF_E + ((i + 1) & 1) * E_BYTES, c + 1, y0, x0, g, e,
-                             coef, x, m32, bsrc);
+      const MftcItem it = mftc_item(G, item, nz1);
+      auto slot = [&](int i) { return smem + off_e(NPL) + (i % NEL) * E_BYTES; };
+      // layers z0-1 .. z0+NEL-3 in flight before the first layer
+      for (int i = 0; i < NEL - 1; ++i) {
+        mftc_stage_own<MODE>(slot(i), it.z0 - 1 + i, it.y0, it.x0, g, e, coef, x, m32, bsrc);
         mftc_commit();
-        const bool ok = mftc_wait(&full[L & 1], (L >> 1) & 1u, abort_f);
+      }
+      int i = 0;
+      for (int c = it.z0 - 1; c < it.z1; ++c, ++L, ++i) {
+        MFTC_MARK(1, 0);
+        unsigned char* S = slot(i);
+        mftc_stage_own<MODE>(slot(i + NEL - 1), c + NEL - 1, it.y0, it.x0, g, e, coef, x, m32,
+                             bsrc);
+        mftc_commit();
+        const bool ok = mftc_wait<WAITK>(&full[L & 1], (L >> 1) & 1u, abort_f);
         if (mftc_group_sync_or(2, fail || !ok)) { fail = true; break; }
+        MFTC_MARK(1, 1);
         tc::fence_after_sync();
         float v[32];
         tc::tmem_ld32(tmem + (L & 1) * 32u + lane_base, v);
         tc::fence_before_sync();
         mftc_arrive(&empty[L & 1]);
-        asm volatile("cp.async.wait_group 1;\n" ::);
+        MFTC_MARK(1, 2);
+        mftc_wait_groups<NEL - 1>();          // this layer's slot has landed
         const float sc = reinterpret_cast<const float*>(S + E_COEF)[e];
         float* Yr = reinterpret_cast<float*>(smem + OFF_Y + (L & 1) * Y_BYTES) + e * YS;
 #pragma unroll
         for (int la = 0; la < 8; ++la)
-          *reinterpret_cast<float4*>(Yr + 4 * la) =
+          *reinterpret_cast<float4*>(Yr + 4 * (la ^ (e & 7))) =
               make_float4(sc * v[3 * la], sc * v[3 * la + 1], sc * v[3 * la + 2], 0.f);
         mftc_group_sync(2);
+        MFTC_MARK(1, 3);
         // node plane c from cell layers c - 1 (Y[(L-1) % 2]) and c (Y[L % 2])
-        if (c >= z0 && e < NPN) {
+        if (c >= it.z0 && e < NPN) {
           const int ly = e % NY, lx = e / NY;
-          const int iy = y0 + ly, ix = x0 + lx;
+          const int iy = it.y0 + ly, ix = it.x0 + lx;
           if (iy < ny1 && ix < nx1) {
             const float* Yc = reinterpret_cast<const float*>(smem + OFF_Y + (L & 1) * Y_BYTES);
             const float* Yb =
@@ -352,7 +416,8 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
             for (int la = 0; la < 8; ++la) {
               const int m = (ly + 1 - hoff(la, 1)) + CY * (lx + 1 - hoff(la, 0));
               const float* Yl = hoff(la, 2) ? Yb : Yc;
-              const float4 w = *reinterpret_cast<const float4*>(Yl + m * YS + 4 * la);
+              const float4 w =
+                  *reinterpret_cast<const float4*>(Yl + m * YS + 4 * (la ^ (m & 7)));
               acc0 += w.x;
               acc1 += w.y;
               acc2 += w.z;
@@ -373,8 +438,45 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
           }
         }
         mftc_group_sync(2);
+        MFTC_MARK(1, 4);
       }
-      asm volatile("cp.async.wait_group 0;\n" ::);
+      mftc_wait_groups<0>();
+    }
+  } else if (tid == 2 * GROUP) {
+    // ------------------------------------------------------------ issuer
+    const uint32_t idesc = tc::idesc_tf32(M, 32);
+    const uint32_t bh = tc::smem_u32(Bs), bl = bh + B_BYTES;
+    uint64_t db[6];
+#pragma unroll
+    for (int s = 0; s < 3; ++s) {
+      db[s] = tc::sdesc(bh + 256u * s, 128u, SBO_B);
+      db[3 + s] = tc::sdesc(bl + 256u * s, 128u, SBO_B);
+    }
+    for (int item = blockIdx.x; item < nitems && !fail; item += gridDim.x) {
+      const MftcItem it = mftc_item(G, item, nz1);
+      for (int c = it.z0 - 1; c < it.z1; ++c, ++L) {
+        MFTC_MARK(0, 3);
+        // the A tile of layer L is built and TMEM buffer L % 2 was drained
+        // (layer L-2)
+        if (!mftc_wait<WAITK>(&ready[L & 1], (L >> 1) & 1u, abort_f) ||
+            !(L < 2 || mftc_wait<WAITK>(&empty[L & 1], ((L - 2) >> 1) & 1u, abort_f))) {
+          fail = true;
+          *const_cast<int*>(abort_f) = 1;
+          break;
+        }
+        tc::fence_after_sync();
+        const uint32_t a0 = tc::smem_u32(smem + OFF_A + (L & 1) * A_BYTES);
+        const uint32_t d = tmem + (L & 1) * 32u;
+#pragma unroll
+        for (int s = 0; s < 6; ++s)
+          tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A), db[s % 3], idesc,
+                       s > 0 ? 1u : 0u);
+#pragma unroll
+        for (int s = 0; s < 3; ++s)
+          tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A), db[3 + s], idesc, 1u);
+        tc::mma_commit(&full[L & 1]);
+        MFTC_MARK(0, 4);
+      }
     }
   }
   if (fail) *const_cast<int*>(abort_f) = 1;

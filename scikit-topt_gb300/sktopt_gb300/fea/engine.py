@@ -100,8 +100,8 @@ class FemEngine:
         N.check(self.lib.topt_fem_set_interpolation(self.h, int(kind)))
 
     def set_mf_kernel(self, kind: int):
-        """Kernel of the matrix-free FP32 level-0 operator: 1 tensor cores
-        (default), 0 FP32 FMA tiles."""
+        """Kernel of the matrix-free FP32 level-0 operator: 0 FP32 FMA tiles
+        (default), 1 tensor cores."""
         N.check(self.lib.topt_fem_set_mf_kernel(self.h, int(kind)))
 
     def mf_error(self) -> int:
