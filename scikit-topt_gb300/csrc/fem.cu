@@ -387,7 +387,7 @@ static int launch_mf_tile(topt_fem* h, const float* x, const float* b, float* y,
 // Tensor-core variant: persistent, two CTAs per SM over (column, z segment)
 // work items; node planes and the drainers' per-layer data in rings of
 // kMfTcNpl and kMfTcNel, suspending mbarrier waits.
-constexpr int kMfTcNpl = 3, kMfTcNel = 3, kMfTcWait = 1;
+constexpr int kMfTcNpl = 6, kMfTcNel = 4, kMfTcWait = 1;
 
 template <int MODE, bool DOT, bool COLMASK>
 static int launch_mf_tc(topt_fem* h, const float* x, const float* b, float* y, int slot) {

@@ -10,26 +10,35 @@
 // node plane of the column form one MMA tile (M = 128 cells): row m holds the
 // cell's 24 DOF values, split into TF32 hi and lo parts, and
 //     Y = [x_hi | x_lo] [K0_hi ; K0_hi] + x_hi K0_lo        (N = 24 -> 32)
-// accumulates in tensor memory (9 MMAs of 128 x 32 x 8).  Row m is then
-// scaled by coef_m and stored to shared memory; each node sums the rows of
-// its 8 cells (two consecutive cell layers) in a fixed order, so the result
-// is deterministic.  Cells on the column's border are computed by both
+// accumulates in tensor memory (9 MMAs of 128 x 32 x 8, the A operand in
+// tensor memory, K0 in shared memory).  Row m is then scaled by coef_m and
+// stored to shared memory; each node sums the rows of its 8 cells (two
+// consecutive cell layers) in a fixed order, so the result is
+// deterministic.  Cells on the column's border are computed by both
 // neighbouring columns (16 x 8 cells for 15 x 7 nodes); cells outside the
-// grid have coefficient 0.
+// grid have coefficient 0.  Shared memory carries only the node halo, K0
+// and the scaled rows (about 0.4 KB per cell): that traffic, not the tensor
+// cores, bounds the operator.
 //
-// Warp roles (288 threads), so that consecutive layers overlap:
-//   builders (warps 0-3): stage node planes (cp.async), split each node's x
-//     once into TF32 hi / lo parts, and build the A tile of layer L into
-//     A[L % 2] once the MMAs of layer L-2 have released it (mbarrier
-//     full[L % 2]); then arrive on mbarrier ready[L % 2];
-//   issuer (warp 8, one lane): waits ready[L % 2] and, for the TMEM buffer,
+// Warp roles (320 threads), so that consecutive layers overlap:
+//   stager (warp 9): loads the column's node planes (x and fixed bits) into
+//     a ring of NPL slots with cp.async, each plane signalled on mbarrier
+//     plane_full[slot] and its slot reused after plane_free[slot];
+//   builders (warps 0-3, lanes 0-127 of tensor memory): once planes c, c+1
+//     have landed and the MMAs of layer L-2 have released A buffer L % 2
+//     (mbarrier full[L % 2]), gather the row of layer L's cell, release
+//     plane c, split the row into TF32 hi / lo parts in registers and store
+//     it to that buffer in tensor memory; then arrive on mbarrier
+//     ready[L % 2];
+//   issuer (warp 8, one lane): waits ready[L % 2] and, for the accumulator,
 //     empty[L % 2] (layer L-2 drained), issues layer L's 9 MMAs and commits
 //     them to full[L % 2];
 //   drainers (warps 4-7, lanes 0-127 of tensor memory): wait full[L % 2],
-//     load the accumulators, release the TMEM buffer (empty[L % 2]), scale
-//     by the cell coefficients, store Y[L % 2] and produce the node plane of
-//     layer L from Y[L % 2] and Y[(L-1) % 2].
-// Builders and drainers each synchronise internally with a named barrier.
+//     load the accumulators, release them (empty[L % 2]), scale by the cell
+//     coefficients, store Y[L % 2] and produce the node plane of layer L
+//     from Y[L % 2] and Y[(L-1) % 2].
+// Drainers synchronise internally with a named barrier; every other hand-off
+// is an mbarrier.
 //
 // Every wait is bounded: on a timeout the CTA sets an abort flag that all
 // roles poll, stops, lets in-flight MMAs drain, writes a NaN into y (the
@@ -49,38 +58,41 @@ constexpr int NHALO = HY * HX;              // 153
 constexpr int M = CY * CX;                  // 128 = MMA rows
 constexpr int NPN = NY * NX;                // 105 output nodes per plane
 constexpr int GROUP = 128;                  // threads per builder / drainer role
-constexpr int THREADS = 2 * GROUP + 32;     // + the issuing warp
+constexpr int THREADS = 2 * GROUP + 64;     // + the issuing and the staging warp
 constexpr uint32_t SBO_A = 12 * 128;        // 48 K columns = 12 core matrices
 constexpr uint32_t SBO_B = 6 * 128;         // 24 K columns
-// Y rows: 8 float4 (one per local node, .w unused), the float4 of local
-// node la of row m stored at position la ^ (m & 7), so that eight
-// consecutive rows touch eight different 16-byte bank groups
-constexpr int YS = 32;
-constexpr uint32_t A_BYTES = M * 48 * 4;    // 24576
+// Y rows: the 24 scaled products of a cell, rows 25 floats apart (an odd
+// stride: consecutive rows start in different banks)
+constexpr int YS = 25;
 constexpr uint32_t B_BYTES = 32 * 24 * 4;   // 3072 per split part
-constexpr uint32_t Y_BYTES = M * YS * 4;    // 16384
-// node planes: per halo node the TF32 hi (x, y, z, 0) and lo parts
-// (x, y, z, 0) as two float4; cp.async lands the raw values (x, y, z and
-// the fixed bits) in the hi slot
-constexpr uint32_t P_BYTES = NHALO * 32;    // 4896
+constexpr uint32_t Y_BYTES = M * YS * 4;    // 12800
+// node planes: per halo node (x, y, z, fixed bits) as one float4
+constexpr uint32_t P_BYTES = NHALO * 16;    // 2448
 // drainers' per-layer slot: coefficients (128), own node x + flags (105 x
 // float4), b or y of the own node (105 x 3)
 constexpr uint32_t E_COEF = 0, E_SELF = M * 4, E_SRC = E_SELF + NPN * 16;
 constexpr uint32_t E_BYTES = (E_SRC + NPN * 12 + 15) & ~15u;
-constexpr uint32_t OFF_A = 0;
-constexpr uint32_t OFF_B = OFF_A + 2 * A_BYTES;
+constexpr uint32_t OFF_B = 0;
 constexpr uint32_t OFF_Y = OFF_B + 2 * B_BYTES;
 constexpr uint32_t OFF_P = OFF_Y + 2 * Y_BYTES;
 // node planes (NPL) and drainer slots (NEL) in rings: plane c + NPL - 1 and
 // the drainers' data of layer c + NEL - 1 are loading while layer c is built
 __host__ __device__ constexpr uint32_t off_e(int NPL) { return OFF_P + NPL * P_BYTES; }
+// mbarriers full, empty, ready [2], plane_full, plane_free [NPL], then the
+// tensor-memory address slot and the abort flag
 __host__ __device__ constexpr uint32_t off_bar(int NPL, int NEL) {
-  return off_e(NPL) + NEL * E_BYTES;   // full, empty, ready [2], tmem slot, abort flag
+  return off_e(NPL) + NEL * E_BYTES;
+}
+__host__ __device__ constexpr uint32_t off_misc(int NPL, int NEL) {
+  return off_bar(NPL, NEL) + 48 + 16 * NPL;
 }
 __host__ __device__ constexpr uint32_t smem_bytes(int NPL, int NEL) {
-  return off_bar(NPL, NEL) + 64;
+  return off_misc(NPL, NEL) + 16;
 }
-constexpr uint32_t TMEM_COLS = 64;
+// tensor memory: accumulators in columns [0, 64) (two buffers of 32), A
+// tiles in [64, 160) (two buffers of 48: x_hi then x_lo)
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t TMEM_A0 = 64;
 constexpr uint32_t WAIT_LIMIT = 1u << 24;
 // image of K0 hi / lo in the B layout, built on the host (2 x 768 floats)
 constexpr int K0_IMAGE_FLOATS = 2 * 32 * 24;
@@ -162,49 +174,6 @@ __device__ __forceinline__ void mftc_arrive(uint64_t* bar) {
 #define MFTC_MARK(role, ev)
 #endif
 
-// Node plane z of the column's halo (builders): x and the fixed-DOF bits
-// into the hi slot of each halo node, zeros outside the grid.
-__device__ __forceinline__ void mftc_stage_plane(float* P, int z, int y0, int x0, int ny1,
-                                                 int nx1, int nz1, int t,
-                                                 const float* __restrict__ x,
-                                                 const uint32_t* __restrict__ m32) {
-  using namespace mftc;
-  const bool zin = z >= 0 && z < nz1;
-  for (int q = t; q < NHALO; q += GROUP) {
-    const int hy = q % HY, hx = q / HY;
-    const int gy = y0 - 1 + hy, gx = x0 - 1 + hx;
-    const bool in = zin && gy >= 0 && gy < ny1 && gx >= 0 && gx < nx1;
-    const int64_t n = in ? (int64_t)gy + (int64_t)ny1 * (gx + (int64_t)nx1 * z) : 0;
-    float* d = P + q * 8;
-    mftc_cp4(d + 0, x + n * 3 + 0, in);
-    mftc_cp4(d + 1, x + n * 3 + 1, in);
-    mftc_cp4(d + 2, x + n * 3 + 2, in);
-    mftc_cp4(d + 3, m32 + n, in);
-  }
-}
-
-// Split a landed plane in place: hi = tf32(x), lo = tf32(x - hi), masked
-// components zeroed first (COLMASK).  Each thread rewrites the halo nodes it
-// staged itself.
-template <bool COLMASK>
-__device__ __forceinline__ void mftc_split_plane(float* P, int t) {
-  using namespace mftc;
-  for (int q = t; q < NHALO; q += GROUP) {
-    float4* d = reinterpret_cast<float4*>(P + q * 8);
-    const float4 v = d[0];
-    float a0 = v.x, a1 = v.y, a2 = v.z;
-    if (COLMASK) {
-      const int mk = __float_as_int(v.w);
-      a0 = (mk & 1) ? 0.f : a0;
-      a1 = (mk & 2) ? 0.f : a1;
-      a2 = (mk & 4) ? 0.f : a2;
-    }
-    const float h0 = tc::to_tf32(a0), h1 = tc::to_tf32(a1), h2 = tc::to_tf32(a2);
-    d[0] = make_float4(h0, h1, h2, 0.f);
-    d[1] = make_float4(tc::to_tf32(a0 - h0), tc::to_tf32(a1 - h1), tc::to_tf32(a2 - h2), 0.f);
-  }
-}
-
 // Drainer e's own data for cell layer c and node plane c: the coefficient of
 // its cell, and (e < 105) its node's x, flags and b / y.  Every thread reads
 // only what it loaded itself.
@@ -256,9 +225,10 @@ __device__ __forceinline__ MftcItem mftc_item(const MfTcGrid& G, int item, int n
   return it;
 }
 
-// 112 registers: two CTAs of 288 threads fit the register file.
+// 96 registers: two CTAs of 320 threads fit the register file (and two
+// CTAs take all 512 columns of tensor memory).
 template <int MODE, bool DOT, bool COLMASK, int NPL, int NEL, int WAITK>
-__global__ void __maxnreg__(112)
+__global__ void __maxnreg__(96)
 k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ coef,
         const uint32_t* __restrict__ m32, const float* __restrict__ x,
         const float* __restrict__ b, float* __restrict__ y, double* partials,
@@ -272,8 +242,10 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + off_bar(NPL, NEL));
   uint64_t* empty = full + 2;
   uint64_t* ready = full + 4;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + off_bar(NPL, NEL) + 48);
-  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + off_bar(NPL, NEL) + 56);
+  uint64_t* pfull = full + 6;
+  uint64_t* pfree = pfull + NPL;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(smem + off_misc(NPL, NEL));
+  volatile int* abort_f = reinterpret_cast<volatile int*>(smem + off_misc(NPL, NEL) + 8);
   const int tid = threadIdx.x, warp = tid >> 5;
   const MfGrid& g = G.g;
   const int ny1 = g.ny + 1, nx1 = g.nx + 1, nz1 = g.nz + 1;
@@ -289,6 +261,10 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
     tc::mbar_init(&empty[1], GROUP);
     tc::mbar_init(&ready[0], GROUP);
     tc::mbar_init(&ready[1], GROUP);
+    for (int i = 0; i < NPL; ++i) {
+      tc::mbar_init(&pfull[i], 32);
+      tc::mbar_init(&pfree[i], GROUP);
+    }
     *abort_f = 0;
     tc::mbar_init_fence();
   }
@@ -306,65 +282,67 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
   if (warp < 4) {
     // ------------------------------------------------------------ builders
     const int t = tid;
-    auto plane = [&](int z) {
-      return reinterpret_cast<float*>(smem + OFF_P + ((z + NPL) % NPL) * P_BYTES);
-    };
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    uint32_t kb = 0;   // running index of the item's first node plane
     for (int item = blockIdx.x; item < nitems && !fail; item += gridDim.x) {
       const MftcItem it = mftc_item(G, item, nz1);
-      // planes z0-1 .. z0+NPL-3 in flight before the first layer
-      for (int z = it.z0 - 1; z <= it.z0 + NPL - 3; ++z) {
-        if (z <= it.z1) mftc_stage_plane(plane(z), z, it.y0, it.x0, ny1, nx1, nz1, t, x, m32);
-        mftc_commit();
-      }
       for (int c = it.z0 - 1; c < it.z1; ++c, ++L) {
         MFTC_MARK(0, 0);
-        mftc_wait_groups<NPL - 3>();          // planes c and c + 1 have landed
-        // the split below rewrites only this thread's own staged nodes; the
-        // barrier makes every builder past layer c-1 before plane c-1's slot
-        // is refilled
-        if (mftc_group_sync_or(1, fail)) { fail = true; break; }
-        const int zp = c + NPL - 1;
-        if (zp <= it.z1)
-          mftc_stage_plane(plane(zp), zp, it.y0, it.x0, ny1, nx1, nz1, t, x, m32);
-        mftc_commit();
-        if (c == it.z0 - 1) mftc_split_plane<COLMASK>(plane(c), t);
-        mftc_split_plane<COLMASK>(plane(c + 1), t);
-        // A[L % 2] is free once the MMAs of layer L-2 have completed
-        const bool ok = L < 2 || mftc_wait<WAITK>(&full[L & 1], ((L - 2) >> 1) & 1u, abort_f);
-        if (mftc_group_sync_or(1, !ok)) { fail = true; break; }
-        MFTC_MARK(0, 1);
-        // A tile of cell layer c: row t = cell (t % 16, t / 16)
+        // planes c and c + 1 (running indices kc, kc + 1) staged by the
+        // staging warp; A buffer L % 2 free once the MMAs of layer L-2 are done
+        const uint32_t kc = kb + (uint32_t)(c - (it.z0 - 1));
+        bool ok = c > it.z0 - 1 ||
+                  mftc_wait<WAITK>(&pfull[kc % NPL], (kc / NPL) & 1u, abort_f);
+        ok = ok && mftc_wait<WAITK>(&pfull[(kc + 1) % NPL], ((kc + 1) / NPL) & 1u, abort_f);
+        ok = ok && (L < 2 || mftc_wait<WAITK>(&full[L & 1], ((L - 2) >> 1) & 1u, abort_f));
+        if (!ok) {
+          fail = true;
+          *const_cast<int*>(abort_f) = 1;
+          break;
+        }
+        MFTC_MARK(0, 2);
+        // row t of layer c: cell (t % 16, t / 16), split into hi | lo
+        float row[48];
         {
           const int rcy = t % CY, rcx = t / CY;
-          const float4* P0 = reinterpret_cast<const float4*>(plane(c));
-          const float4* P1 = reinterpret_cast<const float4*>(plane(c + 1));
-          float xh[24], xl[24];
+          const float4* P0 =
+              reinterpret_cast<const float4*>(smem + OFF_P + (kc % NPL) * P_BYTES);
+          const float4* P1 =
+              reinterpret_cast<const float4*>(smem + OFF_P + ((kc + 1) % NPL) * P_BYTES);
 #pragma unroll
           for (int lb = 0; lb < 8; ++lb) {
             const float4* P = hoff(lb, 2) ? P1 : P0;
-            const int q = (rcx + hoff(lb, 0)) * HY + rcy + hoff(lb, 1);
-            const float4 h = P[2 * q], l = P[2 * q + 1];
-            xh[3 * lb + 0] = h.x;
-            xh[3 * lb + 1] = h.y;
-            xh[3 * lb + 2] = h.z;
-            xl[3 * lb + 0] = l.x;
-            xl[3 * lb + 1] = l.y;
-            xl[3 * lb + 2] = l.z;
-          }
-          unsigned char* A = smem + OFF_A + (L & 1) * A_BYTES;
+            const float4 v = P[(rcx + hoff(lb, 0)) * HY + rcy + hoff(lb, 1)];
+            float a[3] = {v.x, v.y, v.z};
+            if (COLMASK) {
+              const int mk = __float_as_int(v.w);
 #pragma unroll
-          for (int q = 0; q < 6; ++q) {
-            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 4 * q, SBO_A)) =
-                make_float4(xh[4 * q], xh[4 * q + 1], xh[4 * q + 2], xh[4 * q + 3]);
-            *reinterpret_cast<float4*>(A + tc::kmaj_off(t, 24 + 4 * q, SBO_A)) =
-                make_float4(xl[4 * q], xl[4 * q + 1], xl[4 * q + 2], xl[4 * q + 3]);
+              for (int d = 0; d < 3; ++d) a[d] = ((mk >> d) & 1) ? 0.f : a[d];
+            }
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+              const float h = tc::to_tf32(a[d]);
+              row[3 * lb + d] = h;
+              row[24 + 3 * lb + d] = tc::to_tf32(a[d] - h);
+            }
           }
-          tc::fence_async_smem();
         }
+        // plane c is not read again (and, after the item's last layer, nor
+        // is plane c + 1): its slot may be refilled
+        mftc_arrive(&pfree[kc % NPL]);
+        if (c == it.z1 - 1) mftc_arrive(&pfree[(kc + 1) % NPL]);
+        MFTC_MARK(0, 5);
+        tc::fence_after_sync();
+        const uint32_t ta = tmem + TMEM_A0 + (L & 1) * 48u + lane_base;
+        tc::tmem_st16(ta, row);
+        tc::tmem_st16(ta + 16, row + 16);
+        tc::tmem_st16(ta + 32, row + 32);
+        tc::tmem_st_wait();
+        tc::fence_before_sync();
         mftc_arrive(&ready[L & 1]);
-        MFTC_MARK(0, 2);
+        MFTC_MARK(0, 1);
       }
-      mftc_wait_groups<0>();
+      kb += (uint32_t)(it.z1 - it.z0 + 2);
     }
   } else if (warp < 8) {
     // ------------------------------------------------------------ drainers
@@ -389,8 +367,8 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
         if (mftc_group_sync_or(2, fail || !ok)) { fail = true; break; }
         MFTC_MARK(1, 1);
         tc::fence_after_sync();
-        float v[32];
-        tc::tmem_ld32(tmem + (L & 1) * 32u + lane_base, v);
+        float o[32];
+        tc::tmem_ld32(tmem + (L & 1) * 32u + lane_base, o);
         tc::fence_before_sync();
         mftc_arrive(&empty[L & 1]);
         MFTC_MARK(1, 2);
@@ -398,9 +376,7 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
         const float sc = reinterpret_cast<const float*>(S + E_COEF)[e];
         float* Yr = reinterpret_cast<float*>(smem + OFF_Y + (L & 1) * Y_BYTES) + e * YS;
 #pragma unroll
-        for (int la = 0; la < 8; ++la)
-          *reinterpret_cast<float4*>(Yr + 4 * (la ^ (e & 7))) =
-              make_float4(sc * v[3 * la], sc * v[3 * la + 1], sc * v[3 * la + 2], 0.f);
+        for (int k = 0; k < 24; ++k) Yr[k] = sc * o[k];
         mftc_group_sync(2);
         MFTC_MARK(1, 3);
         // node plane c from cell layers c - 1 (Y[(L-1) % 2]) and c (Y[L % 2])
@@ -415,12 +391,10 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
 #pragma unroll
             for (int la = 0; la < 8; ++la) {
               const int m = (ly + 1 - hoff(la, 1)) + CY * (lx + 1 - hoff(la, 0));
-              const float* Yl = hoff(la, 2) ? Yb : Yc;
-              const float4 w =
-                  *reinterpret_cast<const float4*>(Yl + m * YS + 4 * (la ^ (m & 7)));
-              acc0 += w.x;
-              acc1 += w.y;
-              acc2 += w.z;
+              const float* w = (hoff(la, 2) ? Yb : Yc) + m * YS + 3 * la;
+              acc0 += w[0];
+              acc1 += w[1];
+              acc2 += w[2];
             }
             const float4 self = reinterpret_cast<const float4*>(S + E_SELF)[e];
             const float* s3 = reinterpret_cast<const float*>(S + E_SRC) + e * 3;
@@ -465,19 +439,52 @@ k_mf_tc(MfTcGrid G, const float* __restrict__ k0img, const float* __restrict__ c
           break;
         }
         tc::fence_after_sync();
-        const uint32_t a0 = tc::smem_u32(smem + OFF_A + (L & 1) * A_BYTES);
+        const uint32_t a0 = tmem + TMEM_A0 + (L & 1) * 48u;
         const uint32_t d = tmem + (L & 1) * 32u;
 #pragma unroll
         for (int s = 0; s < 6; ++s)
-          tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A), db[s % 3], idesc,
-                       s > 0 ? 1u : 0u);
+          tc::mma_tf32_ta(d, a0 + 8u * s, db[s % 3], idesc, s > 0 ? 1u : 0u);
 #pragma unroll
         for (int s = 0; s < 3; ++s)
-          tc::mma_tf32(d, tc::sdesc(a0 + 256u * s, 128u, SBO_A), db[3 + s], idesc, 1u);
+          tc::mma_tf32_ta(d, a0 + 8u * s, db[3 + s], idesc, 1u);
         tc::mma_commit(&full[L & 1]);
         MFTC_MARK(0, 4);
       }
     }
+  } else if (warp == 9) {
+    // ------------------------------------------------------------ stager
+    const int l = tid - (2 * GROUP + 32);
+    uint32_t k = 0;    // running index of the plane being staged
+    for (int item = blockIdx.x; item < nitems && !fail; item += gridDim.x) {
+      const MftcItem it = mftc_item(G, item, nz1);
+      for (int z = it.z0 - 1; z <= it.z1; ++z, ++k) {
+        // the slot's previous plane (k - NPL) has been released by the builders
+        if (k >= (uint32_t)NPL &&
+            !mftc_wait<WAITK>(&pfree[k % NPL], ((k / NPL) - 1) & 1u, abort_f)) {
+          fail = true;
+          *const_cast<int*>(abort_f) = 1;
+          break;
+        }
+        float* P = reinterpret_cast<float*>(smem + OFF_P + (k % NPL) * P_BYTES);
+        const bool zin = z >= 0 && z < nz1;
+        for (int q = l; q < NHALO; q += 32) {
+          const int hy = q % HY, hx = q / HY;
+          const int gy = it.y0 - 1 + hy, gx = it.x0 - 1 + hx;
+          const bool in = zin && gy >= 0 && gy < ny1 && gx >= 0 && gx < nx1;
+          const int64_t n = in ? (int64_t)gy + (int64_t)ny1 * (gx + (int64_t)nx1 * z) : 0;
+          float* d = P + q * 4;
+          mftc_cp4(d + 0, x + n * 3 + 0, in);
+          mftc_cp4(d + 1, x + n * 3 + 1, in);
+          mftc_cp4(d + 2, x + n * 3 + 2, in);
+          mftc_cp4(d + 3, m32 + n, in);
+        }
+        // one arrival on plane_full per lane once its copies have landed
+        asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(
+                         tc::smem_u32(&pfull[k % NPL]))
+                     : "memory");
+      }
+    }
+    mftc_wait_groups<0>();
   }
   if (fail) *const_cast<int*>(abort_f) = 1;
   __syncthreads();
