@@ -49,7 +49,11 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c1", action="store_true",
+                    help="skip the 60x20x20 same-configuration run against the reference")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
+    ap.add_argument("--nvtx-steps", action="store_true",
+                    help="one NVTX range mixed_<k> per timed iteration (profiler filtering)")
     ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd", "heat_robin",
                                         "multiload"],
                     default=None,
@@ -120,7 +124,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_optimizer(size, precision, max_iters, device):
+def make_optimizer(size, precision, max_iters, device, solver="cg_pyamg"):
     from sktopt_gb300 import tools
     from sktopt_gb300.core import OC_Config, OC_Optimizer
     from sktopt_gb300.mesh import toy_problem
@@ -129,7 +133,7 @@ def make_optimizer(size, precision, max_iters, device):
                     p=tools.SchedulerConfig.constant(target_value=3.0),
                     vol_frac=tools.SchedulerConfig.constant(target_value=0.3),
                     move_limit=tools.SchedulerConfig.constant(target_value=0.2),
-                    E_min_coeff=1e-9, solver_option="cg_pyamg", solver_rtol=1e-8,
+                    E_min_coeff=1e-9, solver_option=solver, solver_rtol=1e-8,
                     precision=precision)
     opt = OC_Optimizer(cfg, toy_problem.cantilever(*size), device=device)
     opt.parameterize()
@@ -156,10 +160,12 @@ def replica_max(t):
     return float(tt.item())
 
 
-def timed_run(opt, warmup, steps, sampler=None, label="steps"):
-    """Warm-up, then `steps` OC iterations timed with CUDA events (NVTX range
-    `label`, for profiler filtering), bracketed by a replica barrier and a
-    device synchronisation on both sides."""
+def timed_run(opt, warmup, steps, sampler=None, label="steps", step_ranges=False):
+    """Warm-up, then `steps` OC iterations timed with CUDA events, bracketed
+    by a replica barrier and a device synchronisation on both sides.  NVTX,
+    for profiler filtering: one range `label` around the window, or with
+    `step_ranges` one range `label_<k>` around each timed iteration k = 1..K
+    instead.  Also returns the launch count of each timed iteration."""
     import torch
     for _ in range(warmup):
         opt.optimize_steps(1)
@@ -172,20 +178,29 @@ def timed_run(opt, warmup, steps, sampler=None, label="steps"):
     if sampler:
         sampler.start()
     torch.cuda.synchronize()
-    torch.cuda.nvtx.range_push(label)
+    if not step_ranges:
+        torch.cuda.nvtx.range_push(label)
     e0.record(s)
     t0 = time.perf_counter()
-    for _ in range(steps):
+    per_step = []
+    for k in range(steps):
+        lk = _native.launch_count()
+        if step_ranges:
+            torch.cuda.nvtx.range_push(f"{label}_{k + 1}")
         opt.optimize_steps(1)
+        if step_ranges:
+            torch.cuda.nvtx.range_pop()
+        per_step.append(_native.launch_count() - lk)
     e1.record(s)
     torch.cuda.synchronize()
-    torch.cuda.nvtx.range_pop()
+    if not step_ranges:
+        torch.cuda.nvtx.range_pop()
     replica_barrier()
     wall = time.perf_counter() - t0
     clocks = sampler.stop() if sampler else None
     l1 = _native.launch_count()
     ms = e0.elapsed_time(e1)
-    return ms, wall, l1 - l0, clocks
+    return ms, wall, l1 - l0, clocks, per_step
 
 
 def _event_time(fn, n=20):
@@ -311,8 +326,9 @@ def run_gpu(args):
     n_full = max(FULL_ITERS, total)
     # mixed precision (headline): W warm-up iterations, K timed
     opt = make_optimizer(size, "mixed", n_full, dev)
-    ms, wall, launches, clocks = timed_run(opt, args.warmup, args.steps, ClockSampler(local),
-                                           label="mixed")
+    ms, wall, launches, clocks, per_step = timed_run(
+        opt, args.warmup, args.steps, ClockSampler(local), label="mixed",
+        step_ranges=args.nvtx_steps)
     phases = None
     if args.phases:
         opt.timer.enabled = True
@@ -403,13 +419,15 @@ def run_gpu(args):
                                "to 1e-8",
                    "parallelism": f"replicas x{world}",
                    "l2": "working set (>4 GB per step) exceeds the 129 MB L2"},
-        "e2e": e2e, "gpu_launches": int(launches),
+        "e2e": e2e, "gpu_launches": int(launches), "gpu_launches_per_step": per_step,
         "roofline": dict(roof, peak_kind=peak_kind),
         "fp64_path": fp64,
         "all_iterations": full,
         "mixed_solver_iters": mixed_stats[-args.steps:],
         "clocks": clocks,
     }
+    if rank == 0 and not args.no_c1:
+        line["c1_same_config"] = c1_same_config(dev)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(size, quick=True)
     if world > 1:
@@ -443,28 +461,74 @@ def cpu_sample(sample, steps_cap=None):
                             vol_frac=oopt.Sched("Constant", 0.3, 0.3),
                             move_limit=oopt.Sched("Constant", 0.2, 0.2),
                             filter_radius=oopt.Sched("Constant", 1.5, 1.5), E_min_coeff=1e-9,
-                            solver="cg_jacobi", rtol=1e-8)
+                            solver="cg_pyamg", rtol=1e-8)
     opt = oopt.OracleOptimizer(cfg, pb, filt, design, fixed, vol)
     t0 = time.perf_counter()
     opt.step()
     return time.perf_counter() - t0, m.nelements
 
 
+CPU_SAMPLE = (48, 16, 16)
+
+
+def _sample_text(sample, ne, sec, scale, cores):
+    return (f"one OC iteration of the oracle (NumPy/SciPy restatement of the reference "
+            f"loop, its cg_pyamg solver option: SciPy CG to 1e-8 preconditioned by the "
+            f"restated smoothed-aggregation V-cycle, converged; W of the Gaussian filter "
+            f"rebuilt per call as the reference does) on the {sample[0]}x{sample[1]}x"
+            f"{sample[2]} cantilever ({ne} elements, {sec:.2f} s), scaled x{scale:.1f} by "
+            f"element count (a lower bound on the full-size time: the AMG-CG iteration "
+            f"count grows with size); host has {cores} cores, the SciPy sparse kernels "
+            f"and the C smoother run on one")
+
+
 def cpu_baseline(size, quick=True):
-    """Oracle iteration on a bounded sample, scaled linearly in the element count
-    (every phase of the reference iteration is linear in it: the capped CG, the
-    per-element filter rebuild, assembly and the bisection)."""
-    sample = (48, 16, 16)
+    """Oracle iteration on a bounded sample of the workload, scaled linearly in
+    the element count."""
     cores = len(os.sched_getaffinity(0))
-    sec, ne = cpu_sample(sample)
+    sec, ne = cpu_sample(CPU_SAMPLE)
     scale = (size[0] * size[1] * size[2]) / ne
     return {"value": round(1.0 / (sec * scale), 6), "unit": "OC iters/s", "cores": 1,
-            "kind": "port",
-            "sample": f"one OC iteration of the NumPy/SciPy restatement on the "
-                      f"{sample[0]}x{sample[1]}x{sample[2]} cantilever ({ne} elements, "
-                      f"{sec:.2f} s; cg_jacobi capped at 1000 iterations, W rebuilt per "
-                      f"filter call), scaled x{scale:.1f} by element count; host has "
-                      f"{cores} cores, SciPy sparse kernels are single-threaded"}
+            "kind": "port", "extrapolated": True,
+            "sample": _sample_text(CPU_SAMPLE, ne, sec, scale, cores)}
+
+
+C1_SIZE, C1_ITERS = (60, 20, 20), 30
+C1_FIXTURE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                          "ref_loop_oc_60x20x20.npz")
+
+
+def c1_same_config(dev):
+    """The 60x20x20 cantilever (24,000 elements, FP64, 30 OC iterations) on
+    the GPU, against the committed run of the reference's own driver loop on
+    the same configuration (tests/golden/ref_loop_oc_60x20x20.npz, written by
+    tests/golden/make_ref_fixtures.py --c1 with the oracle's FEM plugin and
+    SuperLU solves): the compliance of every iteration, and the measured wall
+    time of that CPU run (one x86 core of the machine that wrote it)."""
+    import numpy as np
+    import torch
+    R = np.load(C1_FIXTURE)
+    opt = make_optimizer(C1_SIZE, "fp64", C1_ITERS, dev, solver="spsolve")
+    opt._ensure_state_initialized()
+    opt.fem.engine
+    t, _ = per_iteration_run(opt, C1_ITERS)
+    comp = np.array(opt.recorder.histories["compliance"])
+    err = np.abs(comp - R["compliance"]) / np.abs(R["compliance"])
+    cpu_wall = float(R["wall_s"])
+    gpu_s = sum(t) * 1e-3
+    return {"workload": "60x20x20 hex cantilever, 30 OC iterations, FP64, Gaussian "
+                        "filter r=1.5, p=3, vf=0.3, move 0.2 (the reference's CPU-runnable "
+                        "configuration)",
+            "gpu_it_per_s": round(C1_ITERS / gpu_s, 3),
+            "gpu_ms_per_iter": round(gpu_s * 1e3 / C1_ITERS, 2),
+            "reference_driver_it_per_s": round(C1_ITERS / cpu_wall, 5),
+            "reference_driver_wall_s": round(cpu_wall, 1),
+            "reference_driver_measured": "unmodified reference driver loop (scikit-topt "
+                                         "0.3.9 DensityMethod) with the oracle FEM plugin "
+                                         "and SuperLU (minimum-degree ordering), one x86 "
+                                         "core, when the fixture was written",
+            "speedup_same_config": round(cpu_wall / gpu_s, 1),
+            "compliance_rel_err_vs_reference_max": float(err.max())}
 
 
 def run_reference(args):
@@ -472,7 +536,8 @@ def run_reference(args):
     if rank != 0:
         return
     size = tuple(args.size)
-    sample = (48, 16, 16)
+    sample = CPU_SAMPLE
+    cores = len(os.sched_getaffinity(0))
     for _ in range(args.warmup):
         cpu_sample(sample)
     secs = []
@@ -491,8 +556,9 @@ def run_reference(args):
             "config": {"workload": f"OC loop, {size[0]}x{size[1]}x{size[2]} hex cantilever",
                        "parallelism": "host CPU"},
             "cpu_baseline": {"value": v, "unit": "OC iters/s", "cores": 1, "kind": "port",
-                             "sample": f"{sample[0]}x{sample[1]}x{sample[2]} cantilever, one "
-                                       f"OC iteration per step, scaled x{scale:.1f}"},
+                             "extrapolated": True,
+                             "sample": _sample_text(sample, ne, sum(secs) / len(secs),
+                                                    scale, cores)},
             "e2e": {"value": v, "unit": "OC iters/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

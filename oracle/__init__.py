@@ -29,6 +29,14 @@ Parity status
   matrices, exact volumes, symmetric positive definiteness, filter row
   sums, finite differences) and by fixtures of this restatement
   (``tests/golden/make_golden.py``).
+* Third-party, absent from the reference tree: PyAMG (pyproject.toml:23,
+  ``pyamg >=5.2.1,<6.0.0``), whose ``smoothed_aggregation_solver`` the
+  reference's ``cg_pyamg`` option builds (solver_elastic.py:94-103).
+  ``amg.py`` (with the serial kernels in ``csrc/amg.c``) restates its
+  published algorithm with the 5.x defaults.  Its parity is on the solve:
+  the preconditioned CG reaches the reference's stopping rule and agrees
+  with the direct solve; the hierarchy follows PyAMG's structure but is
+  not compared with PyAMG's (not installable here).
 * SciPy 1.18 (present here) supplies ``spsolve``, ``splu``, ``cg`` and
   ``cKDTree`` as in the reference.
 """

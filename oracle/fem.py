@@ -9,7 +9,7 @@ TEST INFRASTRUCTURE (see ``oracle/__init__.py``).  Restates:
   duplicates summed).
 * ``skfem.enforce`` as used at solver_elastic.py:211 (rows and columns of the
   Dirichlet DOFs zeroed, unit diagonal, prescribed value in the RHS).
-* ``solve_u`` solver_elastic.py:61-143 (spsolve, cg_jacobi), the maxiter rule
+* ``solve_u`` solver_elastic.py:61-143 (spsolve, cg_jacobi, cg_pyamg), the maxiter rule
   solver_elastic.py:201-204, compliance solver_elastic.py:236 and 465.
 * element strain energy solver_elastic.py:470-537 (1/2 u_e^T K_e(rho) u_e),
   heat energy solver_heat.py:256-303, ``dC_drho_simp`` derivatives.py:25-52.
@@ -214,7 +214,8 @@ def default_maxiter(n_dof, maxiter=None):
 
 
 def solve(Ke, Fe, solver="spsolve", rtol=1e-8, maxiter=None):
-    """solver_elastic.py:61-143 for 'spsolve' and 'cg_jacobi'."""
+    """solver_elastic.py:61-143 for 'spsolve', 'cg_jacobi' and 'cg_pyamg'
+    (the smoothed-aggregation preconditioner of ``oracle/amg.py``)."""
     if solver == "spsolve":
         if Fe.ndim == 2:
             lu = spla.splu(Ke.tocsc())
@@ -226,6 +227,13 @@ def solve(Ke, Fe, solver="spsolve", rtol=1e-8, maxiter=None):
         # faster at 60x20x20, the same solution to rounding
         lu = spla.splu(Ke.tocsc(), permc_spec="MMD_AT_PLUS_A")
         return lu.solve(Fe)
+    if solver == "cg_pyamg":
+        from .amg import cg_pyamg
+        mi = default_maxiter(Ke.shape[0], maxiter)
+        if Fe.ndim == 2:
+            return np.stack([cg_pyamg(Ke, Fe[:, j], rtol, mi) for j in range(Fe.shape[1])],
+                            axis=1)
+        return cg_pyamg(Ke, Fe, rtol, mi)
     if solver == "cg_jacobi":
         Minv = 1.0 / Ke.diagonal()
         M = spla.LinearOperator(Ke.shape, matvec=lambda x: Minv * x)
