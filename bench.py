@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
     ap.add_argument("--nvtx-steps", action="store_true",
                     help="one NVTX range mixed_<k> per timed iteration (profiler filtering)")
-    ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd", "heat_robin",
+    ap.add_argument("--probe", choices=["spmv", "solve", "batch", "autograd", "heat_robin", "amg",
                                         "multiload"],
                     default=None,
                     help="profiling target instead of the benchmark")
@@ -860,6 +860,65 @@ def probe_multiload(size=(160, 80, 40), iters=2):
     print(json.dumps(out))
 
 
+def probe_amg(size=(160, 80, 40)):
+    """State solves of the multi-load unstructured configuration (the box of
+    `size` cubes split into 6 jittered P1 tetrahedra each, bottom clamped, 4
+    point-load cases as one block right-hand side) at a seeded random
+    density, to 1e-8, FP64 and mixed, preconditioned by: the GPU-built
+    smoothed-aggregation hierarchy (the logical grid dropped, as for a mesh
+    read from a file), the geometric multigrid of the logical grid, and block
+    Jacobi.  Reports the hierarchy set-up (engine creation), the operator
+    update with the preconditioner refresh, and the solve."""
+    import numpy as np
+    import torch
+    from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
+    from sktopt_gb300.mesh import LinearElasticity, toy_problem
+    from sktopt_gb300.mesh.grid import GridMesh
+    dev = torch.device("cuda", 0)
+    tsk = toy_problem.multi_load_tet(*size, 2.0, 1.0, 1.0, jitter=0.2, seed=0)
+    m = tsk.mesh
+    flat = GridMesh(m.p, m.t, "tet")
+    dn = np.nonzero(m.node_ijk[2] == 0)[0]
+    tsk_flat = LinearElasticity.from_nodes(flat, dn, "all", tsk.neumann_nodes, tsk.neumann_linear,
+                                           np.arange(m.nelements), 1.0, 0.3)
+    g = np.random.default_rng(0)
+    rho = torch.from_numpy(0.05 + 0.95 * g.random(m.nelements)).to(dev)
+    out = {"probe": "amg", "size": list(size), "n_elem": m.nelements, "n_dof": tsk.n_dof,
+           "loads": tsk.n_tasks}
+    for name, task, pre in (("amg", tsk_flat, "mg"), ("geometric_mg", tsk, "mg"),
+                            ("block_jacobi", tsk_flat, "jacobi")):
+        for prec in ("fp64", "mixed"):
+            cfg = LinearSolverConfig(solver="cg_pyamg", rtol=1e-8, precision=prec, precond=pre,
+                                     warm_start=False, maxiter=20000)
+            fem = FEM_SimpLinearElasticity(task, 1e-9, solver_config=cfg, device=dev)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            eng = fem.engine
+            torch.cuda.synchronize()
+            t_setup = time.perf_counter() - t0
+            U = torch.zeros((tsk.n_dof, tsk.n_tasks), dtype=torch.float64, device=dev)
+            rec = {}
+            for rep in range(2):
+                U.zero_()
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fem.build(rho, 3.0)
+                torch.cuda.synchronize()
+                t1 = time.perf_counter()
+                fem.solve_built(U)
+                torch.cuda.synchronize()
+                t2 = time.perf_counter()
+                st = fem.last_stats
+                rec = {"setup_s": round(t_setup, 3), "update_ms": round((t1 - t0) * 1e3, 2),
+                       "solve_ms": round((t2 - t1) * 1e3, 2), "iters": st.iters,
+                       "outer": st.outer, "relres": st.relres, "status": st.status,
+                       "levels": eng.n_levels}
+            out[f"{name}_{prec}"] = rec
+            del fem, eng
+            torch.cuda.empty_cache()
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.probe == "spmv":
@@ -879,6 +938,9 @@ def main():
         return
     if args.probe == "multiload":
         probe_multiload()
+        return
+    if args.probe == "amg":
+        probe_amg(tuple(args.size) if args.size != list(SIZE) else (160, 80, 40))
         return
     if args.impl == "reference":
         run_reference(args)

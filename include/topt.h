@@ -89,6 +89,11 @@ typedef struct topt_fem_desc {
   int32_t mf_level0;          /* mixed, uniform hex elasticity: apply the FP32
                                  fine-level operator matrix-free from the
                                  shared element matrix (no FP32 assembly)    */
+  int32_t amg;                /* no logical grid: 1 = smoothed-aggregation
+                                 multigrid built on the GPU (replaces
+                                 pyamg.smoothed_aggregation_solver of the
+                                 cg_pyamg solve, solver_elastic.py:94-103),
+                                 up to mg_levels levels; 0 = block Jacobi    */
 } topt_fem_desc;
 
 int topt_fem_create(const topt_fem_desc* d, topt_fem** out);
@@ -184,6 +189,20 @@ int topt_fem_spmv(topt_fem* h, int32_t dtype, const void* x, void* y,
 
 /* Copy the enforced FP64 block values (nnzb x bs x bs) to dev memory. */
 int topt_fem_export_values(topt_fem* h, double* vals);
+
+/* Smoothed-aggregation hierarchy (desc.amg = 1), for inspection and tests:
+ * sizes of the transfer from `level` to level + 1 (fine nodes, coarse nodes,
+ * blocks of P), and a HOST copy of it after an update: the aggregate of
+ * every fine node, lambda_max(Dinv A) used for the smoothing, P in CSR
+ * (p_ptr: n_fine + 1, p_col: n_p, p_vals: n_p x bs x bs) and the coarse
+ * operator as a dense (bs n_coarse)^2 row-major matrix (at most 8192 rows).
+ * dtype 1: the FP64 hierarchy; 0: the FP32 one (mixed handles).  The
+ * reference's PyAMG hierarchy (solver_elastic.py:95) has no such export. */
+int topt_fem_amg_sizes(const topt_fem* h, int32_t level, int64_t* n_fine,
+                       int64_t* n_coarse, int64_t* n_p);
+int topt_fem_amg_export(topt_fem* h, int32_t dtype, int32_t level,
+                        int32_t* agg, double* lmax, int64_t* p_ptr,
+                        int32_t* p_col, double* p_vals, double* coarse);
 
 /* Element energies 1/2 coef_e u_e^T Ke u_e (solver_elastic.py:507-537,
  * solver_heat.py:282-303) for every load case and, when dc != NULL, the

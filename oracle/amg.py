@@ -244,3 +244,38 @@ def cg_pyamg(Ke, Fe, rtol=1e-8, maxiter=None, stats=None):
         stats.update(iters=count[0], info=int(info), levels=ml.shapes(),
                      complexity=ml.operator_complexity())
     return u
+
+
+def sa_transfer_from_aggregates(A, agg, cnt_f, bs, lmax, omega=4.0 / 3.0):
+    """The block smoothed-aggregation transfer of the GPU hierarchy, restated
+    for checking it: candidates = the bs per-component translations (zero on
+    fixed DOFs), tentative T(i, a)_cc = sqrt(cnt_f[i, c] / cnt_c[a, c]),
+    P = T - omega / lmax * Dinv A T with the block-diagonal inverse Dinv,
+    coarse operator P^T A P with a unit diagonal on empty coarse DOFs.
+    ``cnt_f``: free finest-level DOFs below each DOF (1 / 0 at level 0).
+    Returns (P, coarse operator, cnt_c)."""
+    A = sp.csr_matrix(A)
+    n = agg.size
+    nc = int(agg.max()) + 1
+    cnt_f = np.asarray(cnt_f, dtype=np.int64).reshape(n, bs)
+    cnt_c = np.zeros((nc, bs), dtype=np.int64)
+    np.add.at(cnt_c, agg, cnt_f)
+    w = np.where(cnt_f > 0, np.sqrt(cnt_f / np.maximum(cnt_c[agg], 1)), 0.0)
+    rows = (np.arange(n)[:, None] * bs + np.arange(bs)[None, :]).ravel()
+    cols = (agg[:, None] * bs + np.arange(bs)[None, :]).ravel()
+    T = sp.csr_matrix((w.ravel(), (rows, cols)), shape=(n * bs, nc * bs))
+    blocks = np.zeros((n, bs, bs))
+    Acoo = A.tocoo()
+    same = (Acoo.row // bs) == (Acoo.col // bs)
+    blocks[Acoo.row[same] // bs, Acoo.row[same] % bs, Acoo.col[same] % bs] = Acoo.data[same]
+    inv = np.zeros_like(blocks)
+    for i in range(n):
+        if abs(np.linalg.det(blocks[i])) > 0:
+            inv[i] = np.linalg.inv(blocks[i])
+    Dinv = sp.block_diag([sp.csr_matrix(b) for b in inv], format="csr")
+    P = sp.csr_matrix(T - (omega / lmax) * (Dinv @ (A @ T)))
+    Ac = (P.T @ A @ P).toarray()
+    d = np.diag(Ac).copy()
+    d[d == 0.0] = 1.0
+    np.fill_diagonal(Ac, d)
+    return P, Ac, cnt_c.ravel()

@@ -62,7 +62,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     def compile_one(src: Path):
         obj = objdir / (src.stem + ".o")
         if src.suffix == ".cu":
-            cmd = [nvcc, *ARCH, "-lineinfo", *common, "-c", str(src), "-o", str(obj)]
+            # -split-compile=0: the device-code optimisation and ptxas of one
+            # translation unit run on all host cores (the engine's largest
+            # unit holds several hundred kernel instantiations)
+            cmd = [nvcc, *ARCH, "-lineinfo", *common, "-split-compile=0", "-c", str(src),
+                   "-o", str(obj)]
         else:
             cmd = [nvcc, *common, "-x", "c++", "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)

@@ -45,7 +45,7 @@ class FemDesc(C.Structure):
         ("grid", C.c_int32 * 3), ("node_ijk", C.POINTER(C.c_int32)),
         ("cell_of_elem", C.POINTER(C.c_int32)),
         ("mixed", C.c_int32), ("mg_levels", C.c_int32), ("mg_coarse_max", C.c_int32),
-        ("mf_level0", C.c_int32),
+        ("mf_level0", C.c_int32), ("amg", C.c_int32),
     ]
 
 
@@ -88,6 +88,9 @@ SIGNATURES = {
     "topt_pattern_export": (C.c_int, [_P, _P, _P, _P, _P]),
     "topt_pattern_free": (None, [_P]),
     "topt_fem_create": (C.c_int, [C.POINTER(FemDesc), C.POINTER(_P)]),
+    "topt_fem_amg_sizes": (C.c_int, [_P, _I32, C.POINTER(_I64), C.POINTER(_I64),
+                                     C.POINTER(_I64)]),
+    "topt_fem_amg_export": (C.c_int, [_P, _I32, _I32, _P, _P, _P, _P, _P, _P]),
     "topt_fem_destroy": (None, [_P]),
     "topt_fem_set_stream": (C.c_int, [_P, _P]),
     "topt_fem_sizes": (C.c_int, [_P, C.POINTER(_I64), C.POINTER(_I64), C.POINTER(_I32)]),

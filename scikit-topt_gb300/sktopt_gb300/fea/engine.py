@@ -33,7 +33,8 @@ class FemEngine:
 
     def __init__(self, mesh: GridMesh, bs: int, ke: np.ndarray, dirichlet_mask: np.ndarray,
                  mixed: bool = False, multigrid: bool = True, mg_levels: int = 16,
-                 mg_coarse_max: int = 200, device=None, matrix_free: bool = True):
+                 mg_coarse_max: int = 200, device=None, matrix_free: bool = True,
+                 amg: bool = True):
         self.lib = N.load()
         self.device = device or default_device()
         self.mesh = mesh
@@ -47,7 +48,9 @@ class FemEngine:
         self._t = np.ascontiguousarray(mesh.t, dtype=np.int32)
         self._ke = ke
         self._mask = np.ascontiguousarray(dirichlet_mask, dtype=np.uint8)
-        # meshes without a logical grid (read from files) run block Jacobi
+        # meshes without a logical grid (read from files) get a
+        # smoothed-aggregation hierarchy built on the GPU (amg) or block Jacobi
+        use_amg = bool(multigrid and amg and not getattr(mesh, "has_grid", True))
         multigrid = multigrid and getattr(mesh, "has_grid", True)
         if multigrid:
             self._ijk = np.ascontiguousarray(mesh.node_ijk, dtype=np.int32)
@@ -67,7 +70,9 @@ class FemEngine:
             d.cell_of_elem = (self._cell.ctypes.data_as(C.POINTER(C.c_int32))
                               if mesh.kind != "hex" else None)
         d.mixed = 1 if mixed else 0
-        d.mg_levels = mg_levels if multigrid else 1
+        d.mg_levels = mg_levels if (multigrid or use_amg) else 1
+        d.amg = 1 if use_amg else 0
+        self.amg = use_amg
         d.mg_coarse_max = mg_coarse_max
         d.mf_level0 = 1 if matrix_free else 0
         h = C.c_void_p()
@@ -108,6 +113,26 @@ class FemEngine:
         out = C.c_int32(0)
         N.check(self.lib.topt_fem_mf_error(self.h, C.byref(out)))
         return out.value
+
+    def amg_export(self, level: int = 0, dtype: int = 1) -> dict:
+        """Host copy of the smoothed-aggregation transfer from `level` to
+        level + 1 after an update: aggregates, lambda_max(Dinv A), P (CSR
+        blocks) and the coarse operator (dense); dtype 1 FP64, 0 FP32."""
+        nf, nc, npb = C.c_int64(), C.c_int64(), C.c_int64()
+        N.check(self.lib.topt_fem_amg_sizes(self.h, int(level), C.byref(nf), C.byref(nc),
+                                            C.byref(npb)))
+        bs = self.bs
+        agg = np.zeros(nf.value, np.int32)
+        lmax = np.zeros(1)
+        p_ptr = np.zeros(nf.value + 1, np.int64)
+        p_col = np.zeros(npb.value, np.int32)
+        p_vals = np.zeros((npb.value, bs, bs))
+        coarse = np.zeros((nc.value * bs, nc.value * bs))
+        N.check(self.lib.topt_fem_amg_export(
+            self.h, int(dtype), int(level), agg.ctypes.data, lmax.ctypes.data,
+            p_ptr.ctypes.data, p_col.ctypes.data, p_vals.ctypes.data, coarse.ctypes.data))
+        return {"agg": agg, "lmax": float(lmax[0]), "p_ptr": p_ptr, "p_col": p_col,
+                "p_vals": p_vals, "coarse": coarse, "n_coarse": nc.value}
 
     def set_extra(self, extra: torch.Tensor | None):
         """Per-element matrices (n_e, nd, nd) added to the level-0 operator

@@ -1,5 +1,6 @@
 """GPU: a design read from a gmsh file (jittered tetrahedra, no logical grid:
-block-Jacobi solves) with surface-traction loads, through the OC loop,
+solves preconditioned by the GPU-built smoothed-aggregation multigrid) with
+surface-traction loads, through the OC loop,
 against the oracle loop on the same mesh and loads.  Two traction groups
 are two load cases (block right-hand side).  Per-iteration compliance 1e-9
 relative (FP64) / 1e-6 (mixed), densities 1e-7 / 1e-5.
@@ -47,7 +48,7 @@ def test_tet_mesh_file_oc_loop_matches_oracle(native_lib, tmp_path, precision):
                     E_min_coeff=1e-9, solver_option="spsolve", precision=precision)
     opt = OC_Optimizer(cfg, tsk, device=_dev())
     opt.parameterize()
-    assert not opt.fem.engine.multigrid
+    assert opt.fem.engine.amg and opt.fem.engine.multigrid
     # oracle: same mesh, Dirichlet nodes, traction loads and design sets
     om = omesh.GridMesh(mesh.p, mesh.t, "tet", None, None, None)
     loads = osurf.surface_forces(om, [mesh.boundaries["neumann_1"],
