@@ -65,7 +65,7 @@ __device__ __forceinline__ int64_t block_excl_scan64(int64_t v, int64_t* sh, int
   return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_tiles(int64_t n, const int32_t* in,
+static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(int64_t n, const int32_t* in,
                                                              int64_t* tile_sum) {
   TOPT_KERNEL_COUNT();
   __shared__ int64_t sh[kScanThreads / 32 + 1];
@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(int64_t n, const in
   if (threadIdx.x == 0) tile_sum[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t ntiles,
+static __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t ntiles,
                                                                  int64_t* tile_sum,
                                                                  int64_t* total) {
   TOPT_KERNEL_COUNT();
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(int64_t ntiles,
   if (threadIdx.x == 0) *total = carry;
 }
 
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(int64_t n, const int32_t* in,
+static __global__ void __launch_bounds__(kScanThreads) k_scan_apply(int64_t n, const int32_t* in,
                                                              const int64_t* tile_sum,
                                                              int64_t* out) {
   TOPT_KERNEL_COUNT();
@@ -139,7 +139,7 @@ __device__ __forceinline__ int64_t sell_pos(const SellT& sp, int64_t i, int k) {
   return ((int64_t)sp.grp_of_slice[i >> 5] + k) * 32 + (i & 31);
 }
 
-__global__ void k_mis_keys(int64_t n, const uint8_t* __restrict__ state,
+static __global__ void k_mis_keys(int64_t n, const uint8_t* __restrict__ state,
                            uint64_t* __restrict__ keys) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -148,7 +148,7 @@ __global__ void k_mis_keys(int64_t n, const uint8_t* __restrict__ state,
 }
 
 // out[i] = max of in[j] over the stored blocks (i, j) of row i (self included).
-__global__ void k_mis_max(SellT sp, const uint64_t* __restrict__ in, uint64_t* __restrict__ out) {
+static __global__ void k_mis_max(SellT sp, const uint64_t* __restrict__ in, uint64_t* __restrict__ out) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < sp.nrows;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -165,7 +165,7 @@ __global__ void k_mis_max(SellT sp, const uint64_t* __restrict__ in, uint64_t* _
 // An undecided node enters the set when the maximum over its distance-2
 // neighbourhood is itself, and leaves it when that maximum is a set node;
 // *left is set while any node stays undecided.
-__global__ void k_mis_update(int64_t n, uint8_t* __restrict__ state,
+static __global__ void k_mis_update(int64_t n, uint8_t* __restrict__ state,
                              const uint64_t* __restrict__ m2, int* __restrict__ left) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -181,7 +181,7 @@ __global__ void k_mis_update(int64_t n, uint8_t* __restrict__ state,
   }
 }
 
-__global__ void k_mis_roots(int64_t n, const uint8_t* __restrict__ state,
+static __global__ void k_mis_roots(int64_t n, const uint8_t* __restrict__ state,
                             int32_t* __restrict__ is_root) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -191,7 +191,7 @@ __global__ void k_mis_roots(int64_t n, const uint8_t* __restrict__ state,
 
 // Roots take their own aggregate; every other node the aggregate of its
 // root neighbour (set nodes are >= 3 apart: at most one), else -1.
-__global__ void k_agg_first(SellT sp, const uint8_t* __restrict__ state,
+static __global__ void k_agg_first(SellT sp, const uint8_t* __restrict__ state,
                             const int64_t* __restrict__ root_id, int32_t* __restrict__ agg) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < sp.nrows;
@@ -215,7 +215,7 @@ __global__ void k_agg_first(SellT sp, const uint8_t* __restrict__ state,
 
 // The remaining nodes join the aggregate of their aggregated neighbour of
 // highest priority (reads the first pass only: order-independent).
-__global__ void k_agg_second(SellT sp, const int32_t* __restrict__ agg1,
+static __global__ void k_agg_second(SellT sp, const int32_t* __restrict__ agg1,
                              int32_t* __restrict__ agg2, int* __restrict__ err) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < sp.nrows;
@@ -257,7 +257,7 @@ __global__ void k_agg_counts(int64_t n, const int32_t* __restrict__ agg,
 }
 
 // Level-0 counts: 1 per free DOF.
-__global__ void k_free_counts(int64_t n, const uint8_t* __restrict__ mask,
+static __global__ void k_free_counts(int64_t n, const uint8_t* __restrict__ mask,
                               int32_t* __restrict__ cnt) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kSymThreads) k_sym(SymArgs g) {
 // ---------------------------------------------------------------- transpose
 // R = P^T pattern: count per coarse node, then fill in fine-row order by
 // a per-coarse-row sort of the (fine node, P entry) pairs.
-__global__ void k_rt_count(int64_t np, const int32_t* __restrict__ p_col,
+static __global__ void k_rt_count(int64_t np, const int32_t* __restrict__ p_col,
                            int32_t* __restrict__ cnt) {
   TOPT_KERNEL_COUNT();
   for (int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; m < np;
@@ -466,7 +466,7 @@ __global__ void k_rt_count(int64_t np, const int32_t* __restrict__ p_col,
     atomicAdd(cnt + p_col[m], 1);
 }
 
-__global__ void k_rt_fill(int64_t np, const int32_t* __restrict__ p_col,
+static __global__ void k_rt_fill(int64_t np, const int32_t* __restrict__ p_col,
                           const int32_t* __restrict__ p_row, const int64_t* __restrict__ r_ptr,
                           int32_t* __restrict__ cursor, int32_t* __restrict__ r_fine,
                           int32_t* __restrict__ r_pent) {
@@ -481,7 +481,7 @@ __global__ void k_rt_fill(int64_t np, const int32_t* __restrict__ p_col,
 }
 
 // Insertion sort of each coarse row by fine node (a node appears once).
-__global__ void k_rt_sort(int64_t nc, const int64_t* __restrict__ r_ptr,
+static __global__ void k_rt_sort(int64_t nc, const int64_t* __restrict__ r_ptr,
                           int32_t* __restrict__ r_fine, int32_t* __restrict__ r_pent) {
   TOPT_KERNEL_COUNT();
   for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < nc;

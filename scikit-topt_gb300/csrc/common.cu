@@ -48,6 +48,11 @@ extern "C" int topt_launch_count(uint64_t* out) {
   unsigned long long d = 0;
   rc = topt::launches_heat(&d);
   if (rc) return rc;
-  *out = (uint64_t)(a + b + c + d);
+  unsigned long long e = 0, f = 0, g = 0, k = 0;
+  if ((rc = topt::launches_spmv(&e))) return rc;
+  if ((rc = topt::launches_amg(&f))) return rc;
+  if ((rc = topt::launches_mf(&g))) return rc;
+  if ((rc = topt::launches_mf_tc(&k))) return rc;
+  *out = (uint64_t)(a + b + c + d + e + f + g + k);
   return TOPT_OK;
 }

@@ -22,14 +22,14 @@ __device__ __forceinline__ double interp_E(int interp, double r, double E0, doub
   return Emin + (E0 - Emin) * (p == 3.0 ? r * r * r : pow(r, p));
 }
 
-__global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+static __global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     b[i] = (float)a[i];
 }
 
-__global__ void k_simp_coef(int64_t n, const double* __restrict__ rho, double E0,
+static __global__ void k_simp_coef(int64_t n, const double* __restrict__ rho, double E0,
                             double Emin, double p, double* __restrict__ c64,
                             float* __restrict__ c32, int interp) {
   TOPT_KERNEL_COUNT();
@@ -61,7 +61,7 @@ struct SellT {
 };
 
 // local node offsets of a hex cell (MeshHex order)
-__constant__ int c_hex_off[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1},
+static __constant__ int c_hex_off[8][3] = {{0, 0, 0}, {0, 1, 0}, {1, 0, 0}, {0, 0, 1},
                                     {1, 1, 0}, {0, 1, 1}, {1, 0, 1}, {1, 1, 1}};
 
 template <int BS>
@@ -649,7 +649,7 @@ __device__ __forceinline__ void mf_node_dinv(const MfGrid& g, const KS& K0,
 }
 
 // All blocks (stored for the power iteration and the generic smoother).
-__global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
+static __global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
                               const float* __restrict__ coef, const uint8_t* __restrict__ mask,
                               float* __restrict__ dinv) {
   TOPT_KERNEL_COUNT();
@@ -668,7 +668,7 @@ __global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
 // inverted diagonal block is recomputed per node from the cell coefficients
 // (the same FP32 arithmetic as k_mf_diag_inv, so the same bits) instead of
 // being read, which saves 36 B per node.  m32: fixed-DOF bits per node.
-__global__ void k_cheb_mf(MfGrid g, const K0f k0, const float* __restrict__ coef,
+static __global__ void k_cheb_mf(MfGrid g, const K0f k0, const float* __restrict__ coef,
                           const uint32_t* __restrict__ m32, ChebEp<float> ep,
                           const float* __restrict__ r) {
   TOPT_KERNEL_COUNT();
@@ -1113,7 +1113,7 @@ __global__ void k_scale(int64_t n, T a, const T* __restrict__ x, T* __restrict__
     y[i] = a * x[i];
 }
 // U += double(d)
-__global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
+static __global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
                                  double* __restrict__ u) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -1121,7 +1121,7 @@ __global__ void k_add_f32_to_f64(int64_t n, const float* __restrict__ d,
     u[i] += (double)d[i];
 }
 // U[fixed DOFs] = 0 (an initial guess of the enforced system).
-__global__ void k_zero_fixed(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
+static __global__ void k_zero_fixed(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
                              double* __restrict__ u) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof * L;
@@ -1129,7 +1129,7 @@ __global__ void k_zero_fixed(int64_t n_dof, int L, const uint8_t* __restrict__ m
     if (mask[i / L]) u[i] = 0.0;
 }
 // F_e: copy of F with fixed DOFs zeroed (enforce's RHS with x = 0).
-__global__ void k_enforce_rhs(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
+static __global__ void k_enforce_rhs(int64_t n_dof, int L, const uint8_t* __restrict__ mask,
                               const double* __restrict__ f, double* __restrict__ fe) {
   TOPT_KERNEL_COUNT();
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_dof * L;
@@ -1453,7 +1453,7 @@ __global__ void k_sell_to_dense(int64_t npos, SellT sp, const T* __restrict__ va
   }
 }
 
-__global__ void __launch_bounds__(1024) k_gauss_jordan_inverse(int n, double* __restrict__ A) {
+static __global__ void __launch_bounds__(1024) k_gauss_jordan_inverse(int n, double* __restrict__ A) {
   TOPT_KERNEL_COUNT();
   __shared__ double pivinv;
   for (int k = 0; k < n; ++k) {

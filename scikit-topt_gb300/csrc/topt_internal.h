@@ -29,6 +29,10 @@ int launches_fem(unsigned long long* out);
 int launches_filter(unsigned long long* out);
 int launches_design(unsigned long long* out);
 int launches_heat(unsigned long long* out);
+int launches_spmv(unsigned long long* out);
+int launches_amg(unsigned long long* out);
+int launches_mf(unsigned long long* out);
+int launches_mf_tc(unsigned long long* out);
 int build_pattern(int64_t n_nodes, int64_t n_elem, int32_t nloc,
                   const int32_t* t, topt_pattern* P);
 

@@ -62,11 +62,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     def compile_one(src: Path):
         obj = objdir / (src.stem + ".o")
         if src.suffix == ".cu":
-            # -split-compile=0: the device-code optimisation and ptxas of one
-            # translation unit run on all host cores (the engine's largest
-            # unit holds several hundred kernel instantiations)
-            cmd = [nvcc, *ARCH, "-lineinfo", *common, "-split-compile=0", "-c", str(src),
-                   "-o", str(obj)]
+            cmd = [nvcc, *ARCH, "-lineinfo", *common, "-c", str(src), "-o", str(obj)]
         else:
             cmd = [nvcc, *common, "-x", "c++", "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -77,7 +73,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         return obj
 
     srcs = sources()
-    with ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    with ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 8, len(srcs)))) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = lib.with_suffix(".so.tmp")
     cmd = [nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
