@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c1", action="store_true",
                     help="skip the 60x20x20 same-configuration run against the reference")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 256 batched designs (sharded over the ranks when N > 1)")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
     ap.add_argument("--nvtx-steps", action="store_true",
                     help="one NVTX range mixed_<k> per timed iteration (profiler filtering)")
@@ -134,7 +136,7 @@ def make_optimizer(size, precision, max_iters, device, solver="cg_pyamg"):
                     vol_frac=tools.SchedulerConfig.constant(target_value=0.3),
                     move_limit=tools.SchedulerConfig.constant(target_value=0.2),
                     E_min_coeff=1e-9, solver_option=solver, solver_rtol=1e-8,
-                    precision=precision)
+                    precision=precision, autotune=True)
     opt = OC_Optimizer(cfg, toy_problem.cantilever(*size), device=device)
     opt.parameterize()
     return opt
@@ -416,7 +418,7 @@ def run_gpu(args):
                                f"({size[0]*size[1]*size[2]} elements), Gaussian filter r=1.5, "
                                "SIMP p=3, vf=0.3, move 0.2, FP64 flexible CG with FP32 "
                                "multigrid and FP32 operator, FP64 residual replacement, "
-                               "to 1e-8",
+                               "to 1e-8; launch shapes from the autotuner",
                    "parallelism": f"replicas x{world}",
                    "l2": "working set (>4 GB per step) exceeds the 129 MB L2"},
         "e2e": e2e, "gpu_launches": int(launches), "gpu_launches_per_step": per_step,
@@ -428,6 +430,8 @@ def run_gpu(args):
     }
     if rank == 0 and not args.no_c1:
         line["c1_same_config"] = c1_same_config(dev)
+    if not args.no_batch:
+        line["batched_designs"] = batch_result(world)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(size, quick=True)
     if world > 1:
@@ -636,46 +640,107 @@ def probe_solve(size):
                       "iters": st.iters, "replacements": st.outer, "relres": st.relres}))
 
 
-def probe_batch(n_designs, iters, workers):
-    """Batched uneven designs: the first `n_designs` cantilevers of the
-    256-design set (seed 0), `iters` mixed OC iterations each, stepped
-    concurrently (one stream per design, `workers` host threads) and then
-    one after another; prints design-iterations per second of both."""
-    import torch
+def _batch_maker(spec, iters, dev, autotune_on):
     from sktopt_gb300 import tools
-    from sktopt_gb300.core import BatchedDesigns, OC_Config, OC_Optimizer
+    from sktopt_gb300.core import OC_Config, OC_Optimizer
     from sktopt_gb300.mesh import toy_problem
-    dev = torch.device("cuda", 0)
+    nx, ny, nz, vf, lf = spec
+
+    def make():
+        cfg = OC_Config(max_iters=iters, filter_type="spacial",
+                        filter_radius=tools.SchedulerConfig.constant(target_value=1.5),
+                        p=tools.SchedulerConfig.constant(target_value=3.0),
+                        vol_frac=tools.SchedulerConfig.constant(target_value=vf),
+                        move_limit=tools.SchedulerConfig.constant(target_value=0.2),
+                        E_min_coeff=1e-9, solver_option="cg_pyamg", precision="mixed",
+                        solver_rtol=1e-8, autotune=autotune_on)
+        return OC_Optimizer(cfg, toy_problem.cantilever(nx, ny, nz, load_frac=lf), device=dev)
+    return make
+
+
+def batch_run(n_designs=256, iters=40, workers=16, check=4, autotune_on=True):
+    """The batched-designs configuration: the first `n_designs` cantilevers of
+    the seeded 256-design set (nx ~ U{16..64}, ny, nz ~ U{8..32}, vf ~
+    U(0.2, 0.5), load position ~ U(0, 1)), `iters` mixed OC iterations each,
+    stepped concurrently (one stream per design, `workers` host threads,
+    launch shapes from the autotuner); then `check` designs (spread over the
+    set) re-run alone and compared bit for bit."""
+    import numpy as np
+    import torch
+    from sktopt_gb300.core import BatchedDesigns, autotune
+    from sktopt_gb300.mesh import toy_problem
+    dev = torch.device("cuda", torch.cuda.current_device())
     specs = toy_problem.batched_cantilever_specs(256, seed=0)[:n_designs]
+    makers = [_batch_maker(s, iters, dev, autotune_on) for s in specs]
+    t0 = time.perf_counter()
+    batch = BatchedDesigns(makers, n_workers=workers, device=dev)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    batch.step(iters)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    idx = sorted(set(int(i) for i in np.linspace(0, n_designs - 1, check)))
+    same = []
+    for i in idx:
+        solo = makers[i]()
+        solo.parameterize()
+        solo.optimize_steps(iters)
+        bo = batch.opts[i]
+        same.append(bool(np.array_equal(bo._state.rho.cpu().numpy(),
+                                        solo._state.rho.cpu().numpy()) and
+                         list(bo.recorder.histories["compliance"]) ==
+                         list(solo.recorder.histories["compliance"])))
+        del solo
+    out = {"workload": f"{n_designs} cantilevers of the seeded set, {iters} mixed OC "
+                       f"iterations each, one stream per design, {workers} host threads",
+           "design_iters_per_s": round(n_designs * iters / dt, 2), "seconds": round(dt, 2),
+           "setup_s": round(t_setup, 2),
+           "elements": int(sum(s[0] * s[1] * s[2] for s in specs)),
+           "solo_bitwise_equal": {str(i): v for i, v in zip(idx, same)},
+           "autotune": autotune.cache() if autotune_on else None}
+    del batch
+    torch.cuda.empty_cache()
+    return out
 
-    def maker(spec):
-        nx, ny, nz, vf, lf = spec
 
-        def make():
-            cfg = OC_Config(max_iters=iters, filter_type="spacial",
-                            filter_radius=tools.SchedulerConfig.constant(target_value=1.5),
-                            p=tools.SchedulerConfig.constant(target_value=3.0),
-                            vol_frac=tools.SchedulerConfig.constant(target_value=vf),
-                            move_limit=tools.SchedulerConfig.constant(target_value=0.2),
-                            E_min_coeff=1e-9, solver_option="cg_pyamg", precision="mixed",
-                            solver_rtol=1e-8)
-            return OC_Optimizer(cfg, toy_problem.cantilever(nx, ny, nz, load_frac=lf),
-                                device=dev)
-        return make
-    out = {"probe": "batch", "designs": n_designs, "iters": iters, "workers": workers,
-           "elements": int(sum(s[0] * s[1] * s[2] for s in specs))}
-    for label, nw in (("concurrent", workers), ("sequential", 1)):
-        batch = BatchedDesigns([maker(s) for s in specs], n_workers=nw, device=dev)
-        batch.step(1)              # warm-up iteration (engines, hierarchies)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        batch.step(iters - 1)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        out[label] = {"design_iters_per_s": round(n_designs * (iters - 1) / dt, 2),
-                      "seconds": round(dt, 3)}
-        del batch
-        torch.cuda.empty_cache()
+def batch_result(world):
+    """The batched-designs key of the bench line.  One rank: `batch_run` on
+    all 256 designs.  N ranks: the designs sharded by cost over the ranks
+    (`run_sharded`, one gather), each rank stepping its share concurrently;
+    the job's design-iterations per second from the slowest rank."""
+    if world <= 1:
+        return batch_run()
+    import torch
+    import torch.distributed as dist
+    from sktopt_gb300.core import run_sharded
+    from sktopt_gb300.mesh import toy_problem
+    rank = dist.get_rank()
+    dev = torch.device("cuda", torch.cuda.current_device())
+    specs = toy_problem.batched_cantilever_specs(256, seed=0)
+    iters = 40
+    makers = [_batch_maker(s, iters, dev, True) for s in specs]
+    costs = [float(s[0] * s[1] * s[2]) for s in specs]
+    replica_barrier()
+    t0 = time.perf_counter()
+    res = run_sharded(makers, costs, iters, rank=rank, world_size=world, n_workers=16)
+    torch.cuda.synchronize()
+    t = replica_max(time.perf_counter() - t0)
+    out = {"workload": f"256 cantilevers of the seeded set, {iters} mixed OC iterations "
+                       f"each, sharded by cost over {world} ranks",
+           "design_iters_per_s": round(256 * iters / t, 2), "seconds": round(t, 2)}
+    if rank == 0:
+        out["designs_gathered"] = len(res)
+    return out
+
+
+def probe_batch(n_designs, iters, workers):
+    """Batched uneven designs: `n_designs` of the set, `iters` mixed OC
+    iterations each, concurrent (with the autotuner) against sequential."""
+    import torch
+    out = {"probe": "batch", "concurrent": batch_run(n_designs, iters, workers, check=2)}
+    out["sequential"] = batch_run(n_designs, iters, 1, check=0, autotune_on=True)
+    torch.cuda.empty_cache()
     print(json.dumps(out))
 
 

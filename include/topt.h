@@ -138,6 +138,30 @@ int topt_fem_set_element_extra(topt_fem* h, const double* extra);
 int topt_fem_set_mf_kernel(topt_fem* h, int32_t kind);
 int topt_fem_mf_error(topt_fem* h, int32_t* mf_error);
 
+/* Launch shapes, for an autotuner (no reference counterpart; none of them
+ * changes what is computed, only the tiling, so results differ by rounding
+ * at most):
+ * - set_mf_tile: node rows per tile of the FP32-FMA fine-level operator,
+ *   16, 27 or 32, 0 = the rule (least padding of ny + 1);
+ * - set_row_mapping: threads per block row of a level's SELL products,
+ *   1 = a warp, 2 = three threads (bs 3), 3 = one thread, 0 = the rule by
+ *   level size;
+ * - get_tuning: the tile in use (0 without the matrix-free operator) and the
+ *   mapping of each of the first n_levels levels (0 for the dense level);
+ * - spmv_level: y = A_level x (one column) with the level's operator of the
+ *   handle's hierarchy precision (FP32 for mixed handles, FP64 otherwise),
+ *   dev pointers; the timing target. */
+int topt_fem_set_mf_tile(topt_fem* h, int32_t ty);
+int topt_fem_set_row_mapping(topt_fem* h, int32_t level, int32_t mapping);
+int topt_fem_get_tuning(const topt_fem* h, int32_t* mf_tile, int32_t* mappings,
+                        int32_t n_levels);
+int topt_fem_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x,
+                        void* y);
+/* Nodes (block rows) of each of the first n_levels levels and whether the
+ * level is the dense coarsest one. */
+int topt_fem_level_sizes(const topt_fem* h, int64_t* n_nodes, int32_t* dense,
+                         int32_t n_levels);
+
 typedef struct topt_solve_opts {
   int32_t method;         /* 0: FP64 PCG.  Mixed (FP32 operator, hierarchy and
                              inner work; FP64 residual, update and dots):

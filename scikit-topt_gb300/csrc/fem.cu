@@ -1466,6 +1466,62 @@ int topt_fem_spmv(topt_fem* h, int32_t dtype, const void* x, void* y, int32_t nr
   return fail(TOPT_BAD_INPUT, "fem_spmv: FP32 operator needs a mixed handle");
 }
 
+int topt_fem_set_mf_tile(topt_fem* h, int32_t ty) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_mf_tile: null handle");
+  if (!(ty == 0 || ty == 16 || ty == 27 || ty == 32))
+    return fail(TOPT_BAD_INPUT, "fem_set_mf_tile: ty must be 0 (automatic), 16, 27 or 32");
+  if (!h->mf) return fail(TOPT_BAD_INPUT, "fem_set_mf_tile: no matrix-free operator");
+  h->mf_ty = ty ? ty : mf_pick_ty(h->mfg.ny + 1);
+  return TOPT_OK;
+}
+
+int topt_fem_set_row_mapping(topt_fem* h, int32_t level, int32_t mapping) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_row_mapping: null handle");
+  if (level < 0 || level >= (int)h->ls.size())
+    return fail(TOPT_BAD_INPUT, "fem_set_row_mapping: no such level");
+  if (mapping < 0 || mapping > 3 || (mapping == 2 && h->bs != 3))
+    return fail(TOPT_BAD_INPUT, "fem_set_row_mapping: mapping must be 0..3 (2 needs bs 3)");
+  h->ls[level].row_map = mapping;
+  return TOPT_OK;
+}
+
+int topt_fem_get_tuning(const topt_fem* h, int32_t* mf_tile, int32_t* mappings,
+                        int32_t n_levels) {
+  if (!h || !mf_tile || (n_levels > 0 && !mappings))
+    return fail(TOPT_BAD_INPUT, "fem_get_tuning: null argument");
+  *mf_tile = h->mf ? h->mf_ty : 0;
+  for (int li = 0; li < n_levels && li < (int)h->ls.size(); ++li)
+    mappings[li] = h->ls[li].dense ? 0 : row_mapping(h->ls[li], h->bs);
+  return TOPT_OK;
+}
+
+int topt_fem_level_sizes(const topt_fem* h, int64_t* n_nodes, int32_t* dense, int32_t n_levels) {
+  if (!h || (n_levels > 0 && (!n_nodes || !dense)))
+    return fail(TOPT_BAD_INPUT, "fem_level_sizes: null argument");
+  for (int li = 0; li < n_levels && li < (int)h->ls.size(); ++li) {
+    n_nodes[li] = h->ls[li].n_nodes;
+    dense[li] = h->ls[li].dense ? 1 : 0;
+  }
+  return TOPT_OK;
+}
+
+int topt_fem_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x, void* y) {
+  if (!h || !x || !y) return fail(TOPT_BAD_INPUT, "fem_spmv_level: null argument");
+  if (!h->assembled) return fail(TOPT_BAD_INPUT, "fem_spmv_level: call topt_fem_update first");
+  if (level < 0 || level >= (int)h->ls.size() || h->ls[level].dense)
+    return fail(TOPT_BAD_INPUT, "fem_spmv_level: no such (non-dense) level");
+  const LevelStruct& L = h->ls[level];
+  if (dtype == TOPT_F32 && h->mixed)
+    return spmv<float>(h, L, h->bs, 1, 0, false,
+                       level == 0 && h->mf ? nullptr : h->h32.lv[level].vals.as<float>(),
+                       (const float*)x, nullptr, (float*)y);
+  if (dtype == TOPT_F64 && !h->mixed)
+    return spmv<double>(h, L, h->bs, 1, 0, false, h->h64.lv[level].vals.as<double>(),
+                        (const double*)x, nullptr, (double*)y);
+  return fail(TOPT_BAD_INPUT, "fem_spmv_level: dtype must be the handle's hierarchy precision "
+                              "(FP32 for mixed handles, FP64 otherwise)");
+}
+
 int topt_fem_export_values(topt_fem* h, double* vals) {
   if (!h || !vals) return fail(TOPT_BAD_INPUT, "fem_export_values: null argument");
   if (!h->assembled) return fail(TOPT_BAD_INPUT, "fem_export_values: not assembled");

@@ -33,6 +33,11 @@ struct LevelStruct {
   bool gal_shared = false;
   bool dense = false;             // coarsest level solved densely
   int ndense = 0;
+  // SELL product row mapping: 0 by level size (warp per row up to
+  // kWarpRowsMax rows, three threads per row up to kRow3Max, then one
+  // thread per row), 1 warp per row, 2 three threads per row (bs 3), 3 one
+  // thread per row (set by topt_fem_set_row_mapping, e.g. by an autotuner)
+  int row_map = 0;
   // smoothed-aggregation transfer to the next level (meshes without a grid;
   // amg_kernels.cuh): np blocks of P, nap of A P, nc_ent of the next level's
   // operator, each with the list of products summed into it
@@ -188,6 +193,9 @@ extern template int spmv<float>(topt_fem*, const LevelStruct&, int, int, int, bo
 extern template int spmv<double>(topt_fem*, const LevelStruct&, int, int, int, bool,
                                  const double*, const double*, const double*, double*, int,
                                  const ChebEp<double>&, bool);
+// spmv.cu: the SELL row mapping a level's products use (1 warp per row, 2
+// three threads per row, 3 one thread per row)
+int row_mapping(const LevelStruct& Ls, int bs);
 // mf.cu: the matrix-free FP32 level-0 operator (same modes as spmv)
 int mf_spmv(topt_fem* h, int L, int mode, bool dot, const float* x, const float* b, float* y,
             int slot, const ChebEp<float>& ep, bool zf);

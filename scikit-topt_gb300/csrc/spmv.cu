@@ -12,14 +12,22 @@ namespace topt {
 
 // Coarse-level product shapes by level size: one warp per block row up to
 // kWarpRowsMax rows, three threads per row (3x3 blocks) up to kRow3Max, one
-// thread per row above.
+// thread per row above; a level's row_map overrides the rule.
 static const int64_t kWarpRowsMax = 16384;
 static const int64_t kRow3Max = 131072;
+
+int row_mapping(const LevelStruct& Ls, int bs) {
+  if (Ls.row_map == 1 || Ls.row_map == 3 || (Ls.row_map == 2 && bs == 3)) return Ls.row_map;
+  if (bs == 3 && Ls.n_nodes > kWarpRowsMax && Ls.n_nodes <= kRow3Max) return 2;
+  if (Ls.n_nodes <= kWarpRowsMax) return 1;
+  return 3;
+}
 
 template <typename T, int BS, int L, int MODE, bool DOT>
 static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const T* x,
                        const T* b, T* y, int red_slot, const ChebEp<T>& ep) {
-  if (BS == 3 && Ls.n_nodes > kWarpRowsMax && Ls.n_nodes <= kRow3Max) {
+  const int map = row_mapping(Ls, BS);
+  if (map == 2) {
     const int g = grid_for((Ls.n_nodes + 63) / 64, 1, h->sm * 16);
     k_sell_spmv3<T, L, MODE, DOT><<<g, 192, 0, h->stream>>>(
         Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),
@@ -27,7 +35,7 @@ static int launch_spmv(topt_fem* h, const LevelStruct& Ls, const T* vals, const 
     TOPT_CHECK_LAUNCH("k_sell_spmv3");
     return TOPT_OK;
   }
-  if (Ls.n_nodes <= kWarpRowsMax) {
+  if (map == 1) {
     const int g = gridsize(h, Ls.n_nodes * 32);
     k_sell_spmv_warp<T, BS, L, MODE, DOT><<<g, kBlock, 0, h->stream>>>(
         Ls.sell, vals, x, b, y, h->red.partials.as<double>(), h->red.ctr(red_slot),

@@ -48,21 +48,8 @@ class BatchedDesigns:
                 opt.fem.engine   # build the FEM handle here, on the design's stream
             self.streams.append(s)
             self.opts.append(opt)
-        self._check_shared_element_matrix()
         self._errors: list[BaseException] = []
         self._lock = threading.Lock()
-
-    def _check_shared_element_matrix(self):
-        ref = None
-        for opt in self.opts:
-            ke = opt.fem.engine._ke
-            if not opt.fem.engine.mixed:
-                continue   # the FP64 operator keeps no constant-bank copy
-            if ref is None:
-                ref = ke
-            elif ke.shape != ref.shape or not np.array_equal(ke, ref):
-                raise ValueError("batched designs must share one element matrix "
-                                 "(the operator's constant bank is process-wide)")
 
     def _run(self, i: int, steps: int):
         try:

@@ -101,6 +101,8 @@ class DensityMethodConfig:
     # design's solution, where 0.05 saves replacements at no extra iterations
     # (a solve from zero prefers 0.1, the solver's own default)
     inner_rtol: float = 5e-2
+    # time the engine's launch shapes once per problem shape (core.autotune)
+    autotune: bool = False
     # OC bisection: FP32 evaluation of each step, FP64 only near a decision
     # edge (same result as the all-FP64 bisection); False = FP64 every step
     bisection_fp32_bracket: bool = True
@@ -117,7 +119,7 @@ class DensityMethodConfig:
     def __post_init__(self):
         self.solver_config = normalize_linear_solver_config(
             self.solver_option, rtol=self.solver_rtol, precision=self.precision,
-            precond=self.precond, inner_rtol=self.inner_rtol)
+            precond=self.precond, inner_rtol=self.inner_rtol, autotune=self.autotune)
 
     def vtu_path(self, iter_num: int):
         """common_density.py:338-339."""

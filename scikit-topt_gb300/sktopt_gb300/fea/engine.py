@@ -114,6 +114,42 @@ class FemEngine:
         N.check(self.lib.topt_fem_mf_error(self.h, C.byref(out)))
         return out.value
 
+    # ------------------------------------------------------------ launch shapes
+    def set_mf_tile(self, ty: int):
+        """Node rows per tile of the FP32-FMA fine-level operator (16, 27,
+        32; 0 = the rule)."""
+        N.check(self.lib.topt_fem_set_mf_tile(self.h, int(ty)))
+
+    def set_row_mapping(self, level: int, mapping: int):
+        """Threads per block row of a level's SELL products (1 warp, 2 three
+        threads, 3 one thread; 0 = the rule by level size)."""
+        N.check(self.lib.topt_fem_set_row_mapping(self.h, int(level), int(mapping)))
+
+    def tuning(self) -> dict:
+        """The launch shapes in use: fine-level tile and per-level mapping."""
+        ty = C.c_int32(0)
+        maps = np.zeros(self.n_levels, np.int32)
+        N.check(self.lib.topt_fem_get_tuning(self.h, C.byref(ty), maps.ctypes.data,
+                                             self.n_levels))
+        return {"mf_tile": ty.value, "row_mapping": maps.tolist()}
+
+    def spmv_level(self, level: int, x: torch.Tensor, y: torch.Tensor):
+        """y = A_level x (one column) in the hierarchy's precision (FP32 for
+        mixed engines, FP64 otherwise)."""
+        self._bind()
+        dt = N.TOPT_F32 if self.mixed else N.TOPT_F64
+        N.check(self.lib.topt_fem_spmv_level(self.h, int(level), dt, C.c_void_p(x.data_ptr()),
+                                             C.c_void_p(y.data_ptr())))
+
+    def level_sizes(self) -> list:
+        """Block rows (nodes) of every level of the hierarchy, and whether the
+        level is the dense coarsest one (as (nodes, dense) pairs)."""
+        nodes = np.zeros(self.n_levels, np.int64)
+        dense = np.zeros(self.n_levels, np.int32)
+        N.check(self.lib.topt_fem_level_sizes(self.h, nodes.ctypes.data, dense.ctypes.data,
+                                              self.n_levels))
+        return [(int(a), bool(b)) for a, b in zip(nodes, dense)]
+
     def amg_export(self, level: int = 0, dtype: int = 1) -> dict:
         """Host copy of the smoothed-aggregation transfer from `level` to
         level + 1 after an update: aggregates, lambda_max(Dinv A), P (CSR

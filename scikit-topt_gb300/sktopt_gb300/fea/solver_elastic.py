@@ -66,6 +66,9 @@ class LinearSolverConfig:
     direct_rtol: float = 1e-12
     mg_levels: int = 16
     mg_coarse_max: int = 200
+    # launch shapes (fine-level tile, SELL row mappings) timed on the device
+    # once per problem shape by core.autotune; False keeps the size rules
+    autotune: bool = False
 
     def resolved_precond(self) -> str:
         if self.precond != "auto":
@@ -148,6 +151,10 @@ class FEM_SimpLinearElasticity:
     def build(self, rho: torch.Tensor, p: float):
         """Assemble K(rho) and refresh the preconditioner."""
         self.engine.update(rho, self.E_max, self.E_min, p)
+        if self.solver_config.autotune and not getattr(self, "_tuned", False):
+            from ..core import autotune
+            self.tuning = autotune.tune(self.engine)
+            self._tuned = True
         self._rho_built = rho
         self._p_built = p
 

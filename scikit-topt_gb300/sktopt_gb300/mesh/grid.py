@@ -289,6 +289,67 @@ def boundary_facets(mesh: GridMesh, predicate=None) -> np.ndarray:
     return bnd.astype(np.int64)
 
 
+def all_facets(mesh: GridMesh):
+    """Every facet once, as rows (element, local face) of its first owner in
+    element order, with a flag per row: True for boundary facets (faces of
+    exactly one element)."""
+    faces = element_faces(mesh.kind)
+    ne = mesh.nelements
+    keys, owner = [], []
+    for f, loc in enumerate(faces):
+        keys.append(np.sort(mesh.t[loc].T, axis=1))
+        owner.append(np.stack([np.arange(ne), np.full(ne, f)], 1))
+    keys = np.concatenate(keys)
+    owner = np.concatenate(owner)
+    order = np.lexsort((owner[:, 1], owner[:, 0]))
+    keys, owner = keys[order], owner[order]
+    _, first, cnt = np.unique(keys, axis=0, return_index=True, return_counts=True)
+    first_sorted = np.sort(first)
+    uniq_cnt = cnt[np.argsort(first)]
+    return owner[first_sorted].astype(np.int64), uniq_cnt == 1
+
+
+def facets_satisfying(mesh: GridMesh, predicate, boundaries_only: bool = False) -> np.ndarray:
+    """scikit-fem ``Mesh.facets_satisfying`` (used at toy_problem.py:66-73):
+    every facet, interior facets once, whose midpoint satisfies the
+    predicate, as rows (element, local face); ``boundaries_only`` keeps the
+    boundary facets (``Mesh.with_boundaries``)."""
+    fac, bnd = all_facets(mesh)
+    if boundaries_only:
+        fac = fac[bnd]
+    mid = mesh.p[:, facet_nodes_of(mesh, fac)].mean(axis=2)
+    return fac[np.asarray(predicate(mid), dtype=bool)]
+
+
+def elements_satisfying(mesh: GridMesh, predicate) -> np.ndarray:
+    """scikit-fem ``Mesh.elements_satisfying`` (toy_problem.py:76-79):
+    elements whose midpoints (the mean of their nodes) satisfy it."""
+    return np.nonzero(np.asarray(predicate(element_centers(mesh)), dtype=bool))[0]
+
+
+def with_boundaries(mesh: GridMesh, boundaries: dict) -> GridMesh:
+    """scikit-fem ``Mesh.with_boundaries`` (toy_problem.py:127): named
+    boundary-facet groups from predicates on the facet midpoints (or facet
+    arrays given as they are); returns a mesh with them added."""
+    out = GridMesh(mesh.p, mesh.t, mesh.kind, mesh.shape, mesh.node_ijk, mesh.cell_of_elem,
+                   mesh.boundaries, mesh.subdomains)
+    for name, b in boundaries.items():
+        out.boundaries[name] = facets_satisfying(mesh, b, boundaries_only=True) \
+            if callable(b) else np.asarray(b, dtype=np.int64).reshape(-1, 2)
+    return out
+
+
+def with_subdomains(mesh: GridMesh, subdomains: dict) -> GridMesh:
+    """scikit-fem ``Mesh.with_subdomains`` (toy_problem.py:129): named element
+    sets (arrays, or predicates on the element midpoints)."""
+    out = GridMesh(mesh.p, mesh.t, mesh.kind, mesh.shape, mesh.node_ijk, mesh.cell_of_elem,
+                   mesh.boundaries, mesh.subdomains)
+    for name, e in subdomains.items():
+        out.subdomains[name] = elements_satisfying(mesh, e) if callable(e) \
+            else np.asarray(e, dtype=np.int64)
+    return out
+
+
 def facets_to_faces(facets: np.ndarray) -> np.ndarray:
     """Hexahedron facets (element, f) as (element, axis, side) rows."""
     facets = np.asarray(facets, dtype=np.int64).reshape(-1, 2)

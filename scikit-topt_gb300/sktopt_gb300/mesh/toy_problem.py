@@ -8,12 +8,17 @@ on the single edge node nearest to y = load_frac * ny.  Built through the
 
 Heat box (100x50x50 workload): T = 0 on the nodes of a centred patch of
 ``patch`` x ``patch`` elements on z = 0 and a uniform volumetric source.
+
+``toy_base`` / ``toy_test`` / ``toy1`` / ``toy1_fine`` / ``toy2``: the
+reference's own toy problems (sktopt/mesh/toy_problem.py:51-144), facets
+and elements selected by their midpoints as scikit-fem does.
 """
 from __future__ import annotations
 
 import numpy as np
 
-from .grid import create_box_hex, create_box_tet
+from .grid import (create_box_hex, create_box_hex_len, create_box_tet, elements_satisfying,
+                   facets_satisfying, get_points_in_range, with_boundaries, with_subdomains)
 from .task import LinearElasticity, LinearHeatConduction
 
 
@@ -101,3 +106,56 @@ def batched_cantilever_specs(n=256, seed=0):
         lf = float(rng.uniform(0.0, 1.0))
         out.append((nx, ny, nz, vf, lf))
     return out
+
+
+def toy_base(mesh_size: float, intorder: int = 2):
+    """toy_problem.py:51-91: an 8 x 6 x 4 box of hexahedra of size
+    `mesh_size`; all DOFs fixed on the facets with midpoints at x <= 0.03; a
+    total force -100 along u^3 spread uniformly over the facets (interior ones
+    included) with midpoints in x in [8 - 1.2, 8.1], y in [2.4, 3.6],
+    z in [4 - 1.2, 4]; E0 = 210e3, nu = 0.3; every element in the design
+    set (less those the loads and supports touch, as from_facets does)."""
+    x_len, y_len, z_len, eps = 8.0, 6.0, 4.0, 1.2
+    mesh = create_box_hex_len(x_len, y_len, z_len, mesh_size)
+    dirichlet_facets = facets_satisfying(
+        mesh, get_points_in_range((0.0, 0.03), (0.0, y_len), (0.0, z_len)))
+    force_facets = facets_satisfying(
+        mesh, get_points_in_range((x_len - eps, x_len + 0.1), (y_len * 2 / 5, y_len * 3 / 5),
+                                  (z_len - eps, z_len)))
+    design_elements = elements_satisfying(
+        mesh, get_points_in_range((0.0, x_len), (0.0, y_len), (0.0, z_len)))
+    return LinearElasticity.from_facets(mesh, dirichlet_facets, "all", force_facets, "u^3",
+                                        -100.0, design_elements, 210e3, 0.30)
+
+
+def toy_test():
+    """toy_problem.py:94-95."""
+    return toy_base(1.0)
+
+
+def toy1():
+    """toy_problem.py:98-99."""
+    return toy_base(0.3)
+
+
+def toy1_fine():
+    """toy_problem.py:102-103."""
+    return toy_base(0.2)
+
+
+def toy2():
+    """toy_problem.py:106-144: an 8 x 8 x 1 plate of hexahedra of size 0.3
+    (27 x 27 x 4), all DOFs fixed on the boundary facets with x <= 0.05, two
+    load cases along u^2 (-1 and +1) on the x = 8 boundary facets with
+    y >= 8 - 0.3 and y <= 0.3, from the mesh tags; E0 = 210e3, nu = 0.3."""
+    x_len, y_len, z_len, mesh_size = 8.0, 8.0, 1.0, 0.3
+    mesh = create_box_hex_len(x_len, y_len, z_len, mesh_size)
+    eps = mesh_size
+    mesh = with_boundaries(mesh, {
+        "dirichlet": get_points_in_range((0.0, 0.05), (0.0, y_len), (0.0, z_len)),
+        "neumann_0": get_points_in_range((x_len, x_len), (y_len - eps, y_len), (0, z_len)),
+        "neumann_1": get_points_in_range((x_len, x_len), (0, eps), (0, z_len)),
+    })
+    mesh = with_subdomains(mesh, {"design": np.arange(mesh.nelements)})
+    return LinearElasticity.from_mesh_tags(mesh, "all", ["u^2", "u^2"], [-1.0, 1.0], 210e3,
+                                           0.30)

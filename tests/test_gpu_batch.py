@@ -45,14 +45,15 @@ def test_batched_designs_match_individual_runs(native_lib):
             list(solo.recorder.histories["compliance"]), spec
 
 
-def test_batched_designs_reject_mixed_element_shapes(native_lib):
+def _stretched(n_iter, autotune=False):
+    """A design with 2 x 1 x 1 cells: another element matrix than the cubes."""
     from sktopt_gb300 import tools
-    from sktopt_gb300.core import BatchedDesigns, OC_Config, OC_Optimizer
+    from sktopt_gb300.core import OC_Config, OC_Optimizer
     from sktopt_gb300.mesh import task
     from sktopt_gb300.mesh.grid import create_box_hex
 
-    def stretched():
-        mesh = create_box_hex(8, 4, 4, hx=2.0)   # 2 x 1 x 1 cells: another element matrix
+    def make():
+        mesh = create_box_hex(8, 4, 4, hx=2.0)
         ijk = mesh.node_ijk
         dn = np.nonzero(ijk[0] == 0)[0]
         ln = np.nonzero((ijk[0] == 8) & (ijk[2] == 0))[0]
@@ -60,12 +61,30 @@ def test_batched_designs_reject_mixed_element_shapes(native_lib):
         f[3 * ln + 2] = -1.0 / ln.size
         tsk = task.LinearElasticity.from_nodes(mesh, dn, "all", ln, [f],
                                                np.arange(mesh.nelements), 1.0, 0.3)
-        cfg = OC_Config(max_iters=2, filter_type="spacial",
+        cfg = OC_Config(max_iters=n_iter, filter_type="spacial",
                         filter_radius=tools.SchedulerConfig.constant(target_value=1.5),
-                        E_min_coeff=1e-9, solver_option="cg_pyamg", precision="mixed")
+                        E_min_coeff=1e-9, solver_option="cg_pyamg", precision="mixed",
+                        autotune=autotune)
         return OC_Optimizer(cfg, tsk, device=_dev())
-    with pytest.raises(ValueError):
-        BatchedDesigns([_make((8, 4, 4, 0.3, 0.5), 2), stretched], device=_dev())
+    return make
+
+
+def test_batched_designs_with_different_element_matrices(native_lib):
+    """Each handle passes its own element matrix to the fine-level operator
+    (a kernel parameter), so designs with different element matrices share a
+    batch and still follow their solo trajectories bit for bit."""
+    from sktopt_gb300.core import BatchedDesigns
+    n_iter = 3
+    makers = [_make((8, 4, 4, 0.3, 0.5), n_iter), _stretched(n_iter)]
+    batch = BatchedDesigns(makers, n_workers=2, device=_dev())
+    batch.step(n_iter)
+    for make, bo in zip(makers, batch.opts):
+        solo = make()
+        solo.parameterize()
+        solo.optimize_steps(n_iter)
+        assert np.array_equal(bo._state.rho.cpu().numpy(), solo._state.rho.cpu().numpy())
+        assert list(bo.recorder.histories["compliance"]) == \
+            list(solo.recorder.histories["compliance"])
 
 
 def test_run_sharded_matches_solo_runs(native_lib):
