@@ -53,6 +53,8 @@ def parse():
                     help="skip the 60x20x20 same-configuration run against the reference")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 256 batched designs (sharded over the ranks when N > 1)")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the multi-load tetrahedral and autograd configurations")
     ap.add_argument("--phases", action="store_true", help="print a per-phase breakdown")
     ap.add_argument("--nvtx-steps", action="store_true",
                     help="one NVTX range mixed_<k> per timed iteration (profiler filtering)")
@@ -432,6 +434,10 @@ def run_gpu(args):
         line["c1_same_config"] = c1_same_config(dev)
     if not args.no_batch:
         line["batched_designs"] = batch_result(world)
+    if rank == 0 and not args.no_extra:
+        # the other configurations at full size, on this rank's GPU
+        line["multi_load_tet"] = probe_multiload()
+        line["autograd"] = probe_autograd()
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(size, quick=True)
     if world > 1:
@@ -795,7 +801,7 @@ def probe_autograd(size=(100, 50, 50)):
             out[f"{phys}_{prec}"] = rec
             del fem
             torch.cuda.empty_cache()
-    print(json.dumps(out))
+    return out
 
 
 def probe_heat_robin(size=(200, 200, 25), small=(40, 40, 5), iters=5, warmup=3):
@@ -922,7 +928,7 @@ def probe_multiload(size=(160, 80, 40), iters=2):
                                           for a, b in zip(hist["mixed"], hist["fp64"])]
     out["speedup_mixed_vs_fp64"] = round(out["fp64"]["ms_per_iter"] /
                                          out["mixed"]["ms_per_iter"], 2)
-    print(json.dumps(out))
+    return out
 
 
 def probe_amg(size=(160, 80, 40)):
@@ -996,13 +1002,13 @@ def main():
         probe_batch(32, 6, 16)
         return
     if args.probe == "autograd":
-        probe_autograd()
+        print(json.dumps(probe_autograd()))
         return
     if args.probe == "heat_robin":
         probe_heat_robin()
         return
     if args.probe == "multiload":
-        probe_multiload()
+        print(json.dumps(probe_multiload()))
         return
     if args.probe == "amg":
         probe_amg(tuple(args.size) if args.size != list(SIZE) else (160, 80, 40))

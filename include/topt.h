@@ -236,6 +236,11 @@ int topt_fem_amg_export(topt_fem* h, int32_t dtype, int32_t level,
 int topt_fem_energy(topt_fem* h, const double* U, int32_t nrhs,
                     const double* rho, double E0, double Emin, double p,
                     const double* dh, double* energy, double* dc);
+/* Arithmetic of topt_fem_energy: fp32 = 1 computes u_e^T Ke u_e in FP32 from
+ * the FP64 displacements (shifted by node 0) and returns FP64 energies and
+ * sensitivities (relative error ~1e-7; the elasticity plugin's mixed path);
+ * fp32 = 0: FP64 throughout (the default). */
+int topt_fem_set_energy_precision(topt_fem* h, int32_t fp32);
 
 /* ------------------------------------------------------------------------
  * Gaussian density filter (SpacialFilter, sktopt/filters/spacial.py:106-166;

@@ -1652,23 +1652,39 @@ int topt_fem_energy(topt_fem* h, const double* U, int32_t nrhs, const double* rh
   if (nrhs < 1 || nrhs > 8) return fail(TOPT_BAD_INPUT, "fem_energy: nrhs must be 1..8");
   const int nd = h->bs * h->nloc;
   const int64_t stride = h->n_ke == 1 ? 0 : (int64_t)nd * nd;
-  const size_t sh = stride == 0 ? sizeof(double) * nd * nd : 0;
   const int g = gridsize(h, h->n_elem, 128);
   const int32_t* t = h->ls[0].t.as<int32_t>();
-  const double* ke = h->ke64.as<double>();
-  if (h->bs == 3 && h->nloc == 8)
-    k_energy<3, 8><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc, h->interp);
-  else if (h->bs == 3)
-    k_energy<3, 4><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc, h->interp);
-  else if (h->nloc == 8)
-    k_energy<1, 8><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc, h->interp);
+#define TOPT_ENERGY(TC, KE)                                                                    \
+  do {                                                                                         \
+    const size_t sh = stride == 0 ? sizeof(TC) * nd * nd : 0;                                  \
+    const TC* ke = KE;                                                                         \
+    if (h->bs == 3 && h->nloc == 8)                                                            \
+      k_energy<3, 8, TC><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, \
+                                                    Emin, p, dh, energy, dc, h->interp);       \
+    else if (h->bs == 3)                                                                       \
+      k_energy<3, 4, TC><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, \
+                                                    Emin, p, dh, energy, dc, h->interp);       \
+    else if (h->nloc == 8)                                                                     \
+      k_energy<1, 8, TC><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, \
+                                                    Emin, p, dh, energy, dc, h->interp);       \
+    else                                                                                       \
+      k_energy<1, 4, TC><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, \
+                                                    Emin, p, dh, energy, dc, h->interp);       \
+  } while (0)
+  if (h->energy32)
+    TOPT_ENERGY(float, h->ke32.as<float>());
   else
-    k_energy<1, 4><<<g, 128, sh, h->stream>>>(h->n_elem, nrhs, t, ke, stride, U, rho, E0, Emin,
-                                              p, dh, energy, dc, h->interp);
+    TOPT_ENERGY(double, h->ke64.as<double>());
+#undef TOPT_ENERGY
   TOPT_CHECK_LAUNCH("k_energy");
+  return TOPT_OK;
+}
+
+int topt_fem_set_energy_precision(topt_fem* h, int32_t fp32) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_energy_precision: null handle");
+  if (fp32 != 0 && fp32 != 1)
+    return fail(TOPT_BAD_INPUT, "fem_set_energy_precision: fp32 must be 0 or 1");
+  h->energy32 = fp32 != 0;
   return TOPT_OK;
 }
 

@@ -1513,23 +1513,23 @@ __global__ void k_dense_matvec(int n, const T* __restrict__ Ainv, const T* __res
 // Element energies and compliance sensitivities (one thread per element):
 // q = u_e^T Ke u_e, energy = 1/2 coef q (solver_elastic.py:470-537),
 // dc = dC_drho_simp(rho, energy) (derivatives.py:25-52) times dh.
-template <int BS, int NLOC>
+template <int BS, int NLOC, typename TC>
 __global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
-                         const double* __restrict__ ke, int64_t ke_stride,
+                         const TC* __restrict__ ke, int64_t ke_stride,
                          const double* __restrict__ U, const double* __restrict__ rho,
                          double E0, double Emin, double p, const double* __restrict__ dh,
                          double* __restrict__ energy, double* __restrict__ dc, int interp) {
   TOPT_KERNEL_COUNT();
   constexpr int ND = BS * NLOC;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* kes = reinterpret_cast<double*>(smem_raw);
+  TC* kes = reinterpret_cast<TC*>(smem_raw);
   if (ke_stride == 0) {
     for (int i = threadIdx.x; i < ND * ND; i += blockDim.x) kes[i] = ke[i];
     __syncthreads();
   }
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    const double* K = ke_stride ? ke + e * ke_stride : kes;
+    const TC* K = ke_stride ? ke + e * ke_stride : kes;
     int64_t node[NLOC];
 #pragma unroll
     for (int a = 0; a < NLOC; ++a) node[a] = t[(int64_t)a * ne + e];
@@ -1551,23 +1551,24 @@ __global__ void k_energy(int64_t ne, int L, const int32_t* __restrict__ t,
       // u - u(node 0) per component: a translation lies in the null space of
       // every element matrix, and the shift keeps u^T K u from cancelling
       // when the field carries a large offset (a prescribed temperature)
-      double u[ND], u0[BS];
+      TC u[ND];
+      double u0[BS];
 #pragma unroll
       for (int c = 0; c < BS; ++c) u0[c] = U[(node[0] * BS + c) * L + j];
 #pragma unroll
       for (int a = 0; a < NLOC; ++a)
 #pragma unroll
-        for (int c = 0; c < BS; ++c) u[a * BS + c] = U[(node[a] * BS + c) * L + j] - u0[c];
-      double q = 0.0;
+        for (int c = 0; c < BS; ++c)
+          u[a * BS + c] = (TC)(U[(node[a] * BS + c) * L + j] - u0[c]);
+      TC q = TC(0);
 #pragma unroll
       for (int i = 0; i < ND; ++i) {
-        double s = 0.5 * K[i * ND + i] * u[i];
+        TC s = TC(0.5) * K[i * ND + i] * u[i];
 #pragma unroll
         for (int k = i + 1; k < ND; ++k) s += K[i * ND + k] * u[k];
         q += u[i] * s;
       }
-      q *= 2.0;
-      const double en = 0.5 * coef * q;
+      const double en = coef * (double)q;
       if (energy) energy[e * L + j] = en;
       if (dc) dc[e * L + j] = (-2.0 * en * dE / Ec) * h;
     }

@@ -120,6 +120,9 @@ struct topt_fem {
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   int interp = 0;                      // 0 SIMP, 1 RAMP, 2 RAMP / SIMP-form sensitivity
+  // element energies and sensitivities in FP32 arithmetic (the elasticity
+  // plugin's mixed path: FP64 stays in the residual, the update and the dots)
+  bool energy32 = false;
   // per-element matrices added to coef_e Ke at level 0 (caller's device
   // buffer, n_elem x (bs nloc)^2 FP64; the heat plugin's Robin terms)
   const double* extra64 = nullptr;

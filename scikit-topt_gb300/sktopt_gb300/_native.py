@@ -92,6 +92,7 @@ SIGNATURES = {
                                      C.POINTER(_I64)]),
     "topt_fem_amg_export": (C.c_int, [_P, _I32, _I32, _P, _P, _P, _P, _P, _P]),
     "topt_fem_set_mf_tile": (C.c_int, [_P, _I32]),
+    "topt_fem_set_energy_precision": (C.c_int, [_P, _I32]),
     "topt_fem_set_row_mapping": (C.c_int, [_P, _I32, _I32]),
     "topt_fem_get_tuning": (C.c_int, [_P, C.POINTER(_I32), _P, _I32]),
     "topt_fem_spmv_level": (C.c_int, [_P, _I32, _I32, _P, _P]),

@@ -114,6 +114,11 @@ class FemEngine:
         N.check(self.lib.topt_fem_mf_error(self.h, C.byref(out)))
         return out.value
 
+    def set_energy_precision(self, fp32: bool):
+        """Element energies / sensitivities in FP32 arithmetic (the default of
+        mixed engines) or FP64."""
+        N.check(self.lib.topt_fem_set_energy_precision(self.h, 1 if fp32 else 0))
+
     # ------------------------------------------------------------ launch shapes
     def set_mf_tile(self, ty: int):
         """Node rows per tile of the FP32-FMA fine-level operator (16, 27,
