@@ -238,8 +238,8 @@ int topt_fem_energy(topt_fem* h, const double* U, int32_t nrhs,
                     const double* dh, double* energy, double* dc);
 /* Arithmetic of topt_fem_energy: fp32 = 1 computes u_e^T Ke u_e in FP32 from
  * the FP64 displacements (shifted by node 0) and returns FP64 energies and
- * sensitivities (relative error ~1e-7; the elasticity plugin's mixed path);
- * fp32 = 0: FP64 throughout (the default). */
+ * sensitivities (1.2e-6 relative L2 on the sensitivities of the 240x80x80
+ * loop); fp32 = 0: FP64 throughout (the default). */
 int topt_fem_set_energy_precision(topt_fem* h, int32_t fp32);
 
 /* ------------------------------------------------------------------------

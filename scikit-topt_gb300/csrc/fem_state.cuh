@@ -120,8 +120,9 @@ struct topt_fem {
   int lmax_alloc = 0;
   double E0 = 1.0, Emin = 0.0, p = 3.0;
   int interp = 0;                      // 0 SIMP, 1 RAMP, 2 RAMP / SIMP-form sensitivity
-  // element energies and sensitivities in FP32 arithmetic (the elasticity
-  // plugin's mixed path: FP64 stays in the residual, the update and the dots)
+  // element energies and sensitivities in FP32 arithmetic (opt-in: measured
+  // 1.2e-6 relative L2 on the sensitivities of the 240x80x80 loop, above the
+  // 1e-6 gate, so the default stays FP64)
   bool energy32 = false;
   // per-element matrices added to coef_e Ke at level 0 (caller's device
   // buffer, n_elem x (bs nloc)^2 FP64; the heat plugin's Robin terms)

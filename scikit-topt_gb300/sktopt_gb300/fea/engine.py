@@ -115,8 +115,8 @@ class FemEngine:
         return out.value
 
     def set_energy_precision(self, fp32: bool):
-        """Element energies / sensitivities in FP32 arithmetic (the default of
-        mixed engines) or FP64."""
+        """Element energies / sensitivities in FP32 arithmetic (opt-in) or
+        FP64 (the default)."""
         N.check(self.lib.topt_fem_set_energy_precision(self.h, 1 if fp32 else 0))
 
     # ------------------------------------------------------------ launch shapes

@@ -140,9 +140,6 @@ class FEM_SimpLinearElasticity:
                 mg_levels=cfg.mg_levels, mg_coarse_max=cfg.mg_coarse_max,
                 device=self.device)
             self._engine.set_interpolation(self.interp_kind)
-            # mixed path: element energies and sensitivities in FP32 (FP64
-            # stays in the residual, the solution update and the dots)
-            self._engine.set_energy_precision(cfg.precision == "mixed")
             F = np.column_stack(self.task.neumann_linear)
             self._F = torch.from_numpy(np.ascontiguousarray(F)).to(self.device)
         return self._engine
