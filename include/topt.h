@@ -366,11 +366,13 @@ int topt_node_to_elem(int64_t n_elem, int32_t nloc, const int32_t* t, const doub
                       int32_t clamp_nonpositive, double* out, void* stream);
 
 /* ------------------------------------------------------------------------
- * Heat plugin on hexahedral meshes (FEM_SimpLinearHeatConduction,
- * sktopt/fea/solver_heat.py:306-625, 705-980): Robin terms, heat-exchange
- * objective and adjoint load, explicit Robin gradient, grad T . grad lam.
- * Cells must be axis-aligned boxes; volume integrals use the 2x2x2 Gauss
- * rule.  Vectors are dev, n_nodes (x L row-major for several columns).
+ * Heat plugin on hexahedral and P1 tetrahedral meshes
+ * (FEM_SimpLinearHeatConduction, sktopt/fea/solver_heat.py:306-625,
+ * 705-980): Robin terms, heat-exchange objective and adjoint load, explicit
+ * Robin gradient, grad T . grad lam.  Hexahedra must be axis-aligned boxes
+ * (volume integrals with the 2x2x2 Gauss rule); tetrahedra take the 4-point
+ * degree-2 rule.  Vectors are dev, n_nodes (x L row-major for several
+ * columns).
  * ---------------------------------------------------------------------- */
 typedef struct topt_heat topt_heat;
 /* t: host, 8 x n_elem (row a = local node a, MeshHex order); p: host,
@@ -380,11 +382,17 @@ typedef struct topt_heat topt_heat;
  * t[a][e] the density of element e. */
 int topt_heat_create(int64_t n_nodes, int64_t n_elem, const int32_t* t, const double* p,
                      int32_t pairing, topt_heat** out);
+/* The same for nloc = 8 (hexahedra, as above) or nloc = 4 (P1 tetrahedra:
+ * volume forms with the 4-point degree-2 rule of a basis with intorder 2;
+ * pairing 0 then gives node t[a][e] rho[(a n_elem + e) / 4]). */
+int topt_heat_create_mesh(int64_t n_nodes, int64_t n_elem, int32_t nloc,
+                          const int32_t* t, const double* p, int32_t pairing,
+                          topt_heat** out);
 void topt_heat_destroy(topt_heat* h);
 int topt_heat_set_stream(topt_heat* h, void* cuda_stream);
 /* Surface Robin matrices h int N_a N_b over the Robin facets
- * (assemble_surface_robin task_heat.py:60-139), one 8 x 8 per facet in the
- * owning element's local numbering.  elems, mats: host. */
+ * (assemble_surface_robin task_heat.py:60-139), one nloc x nloc per facet
+ * in the owning element's local numbering.  elems, mats: host. */
 int topt_heat_set_surface(topt_heat* h, int64_t n_faces, const int32_t* elems,
                           const double* mats);
 /* rho_node = the nodal average of the element densities rho. */

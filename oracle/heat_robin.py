@@ -1,8 +1,11 @@
 """Oracle of the heat plugin's Robin terms and heat objectives (TEST INFRASTRUCTURE).
 
 Only ``tests/``, the smoke entry and the bench's CPU legs use this module, as
-the checker.  It restates, on hexahedral meshes, with the 2x2x2 Gauss rule of
-the element matrices (basis intorder=2) for every volume form:
+the checker.  It restates, on hexahedral meshes with the 2x2x2 Gauss rule of
+the element matrices (basis intorder=2) and on P1 tetrahedra with the
+4-point degree-2 rule (intorder=2: barycentric points (a, b, b, b),
+a = (5 + 3 sqrt 5) / 20, b = (5 - sqrt 5) / 20, weights 1/4 of the volume)
+for every volume form:
 
 * ``_element_to_nodal_average`` sktopt/fea/solver_heat.py:600-613 and the
   same average inside ``objectives_multi_load`` 730-737: ``np.add.at`` over
@@ -67,6 +70,32 @@ def hex_quadrature(mesh):
     return N, dN, w[None, :] * det
 
 
+_TA = (5.0 + 3.0 * np.sqrt(5.0)) / 20.0
+_TB = (5.0 - np.sqrt(5.0)) / 20.0
+
+
+def tet_quadrature(mesh):
+    """Shape values N (4, 4) at the 4-point degree-2 rule, the constant
+    physical gradients dN (ne, 4, 4, 3) and weights w*detJ (ne, 4) of every
+    P1 tetrahedron."""
+    N = np.full((4, 4), _TB)
+    np.fill_diagonal(N, _TA)                                       # point q: (a at node q)
+    c = mesh.p[:, mesh.t]                                          # (3, 4, ne)
+    J = np.stack([c[:, 1] - c[:, 0], c[:, 2] - c[:, 0], c[:, 3] - c[:, 0]], axis=2)  # (3, ne, 3)
+    J = np.transpose(J, (1, 0, 2))                                 # (ne, 3, 3): dx_d / dxi_k
+    det = np.linalg.det(J)
+    Jinv = np.linalg.inv(J)
+    gr = np.array([[-1.0, -1.0, -1.0], [1.0, 0, 0], [0, 1.0, 0], [0, 0, 1.0]])  # dN/dxi
+    g = np.einsum("ak,ekd->ead", gr, Jinv)                         # (ne, 4, 3)
+    dN = np.broadcast_to(g[:, None], (g.shape[0], 4, 4, 3)).copy()
+    wd = np.repeat((np.abs(det) / 24.0)[:, None], 4, axis=1)
+    return N, dN, wd
+
+
+def element_quadrature(mesh):
+    return hex_quadrature(mesh) if mesh.kind == "hex" else tet_quadrature(mesh)
+
+
 def nodal_average(mesh, rho, pairing="reference"):
     """solver_heat.py:600-613.  Returns (rho_nodal, count)."""
     t = mesh.t
@@ -97,9 +126,9 @@ def _scatter_vec(mesh, fe):
 
 def _assemble_mats(mesh, Me):
     t = mesh.t
-    ne = t.shape[1]
-    rows = np.broadcast_to(t.T[:, :, None], (ne, 8, 8)).reshape(-1)
-    cols = np.broadcast_to(t.T[:, None, :], (ne, 8, 8)).reshape(-1)
+    nloc, ne = t.shape
+    rows = np.broadcast_to(t.T[:, :, None], (ne, nloc, nloc)).reshape(-1)
+    cols = np.broadcast_to(t.T[:, None, :], (ne, nloc, nloc)).reshape(-1)
     n = mesh.nnodes
     K = sp.coo_matrix((Me.reshape(-1), (rows, cols)), shape=(n, n)).tocsr()
     K.sum_duplicates()
@@ -125,12 +154,37 @@ def hex_face_nodes(axis, side):
     return [a for a in range(8) if HEX_OFFSETS[a][axis] == side]
 
 
+TET_FACES = [[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]]
+
+
+def surface_robin_tet(mesh, faces, h, t_env):
+    """assemble_surface_robin task_heat.py:60-139 on triangle facets, rows
+    (element, local face): h int N_a N_b = h A / 12 (1 + delta_ab) and
+    h T_env int N_a = h T_env A / 3 (exact)."""
+    nf = faces.shape[0]
+    Me = np.zeros((nf, 4, 4))
+    load = np.zeros(mesh.nnodes)
+    for k, (e, f) in enumerate(faces):
+        loc = TET_FACES[f]
+        X = mesh.p[:, mesh.t[loc, e]]
+        A = 0.5 * np.linalg.norm(np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]))
+        for i, a in enumerate(loc):
+            for j, b in enumerate(loc):
+                Me[k, a, b] = h * A / 12.0 * (2.0 if i == j else 1.0)
+        np.add.at(load, mesh.t[loc, e], h * t_env * A / 3.0)
+    return Me, load
+
+
 def surface_robin(mesh, faces, h, t_env):
     """assemble_surface_robin task_heat.py:60-139 for one facet group.
 
-    faces: (nf, 3) rows (element, axis, side).  Returns per-face element
-    matrices (nf, 8, 8) (zero outside the face's nodes) and the nodal load.
-    2x2 Gauss on the bilinear face map (exact for these polynomial forms)."""
+    faces: (nf, 3) rows (element, axis, side) on hexahedra, (nf, 2) rows
+    (element, local face) on tetrahedra.  Returns per-face element matrices
+    (nf, nloc, nloc) (zero outside the face's nodes) and the nodal load.
+    Hexahedra: 2x2 Gauss on the bilinear face map (exact for these
+    polynomial forms)."""
+    if mesh.kind != "hex":
+        return surface_robin_tet(mesh, faces, h, t_env)
     nf = faces.shape[0]
     Me = np.zeros((nf, 8, 8))
     load = np.zeros(mesh.nnodes)
@@ -232,7 +286,8 @@ def grad_dot(mesh, Q, X, Y):
 
 
 class HeatRobinProblem:
-    """FEM_SimpLinearHeatConduction (solver_heat.py:628-980) on a hex mesh."""
+    """FEM_SimpLinearHeatConduction (solver_heat.py:628-980) on a hex or P1
+    tet mesh."""
 
     def __init__(self, mesh, dirichlet_nodes, dirichlet_values, k0=1.0,
                  robin_faces=None, robin_coefficient=None, robin_bc_value=None,
@@ -246,8 +301,11 @@ class HeatRobinProblem:
         vals = dirichlet_values if isinstance(dirichlet_values, (list, tuple)) \
             else [dirichlet_values]
         self.values = [float(v) for v in vals]
-        c = mesh.p[:, mesh.t[:, 0]]
-        _, self.Kloc = fem.hex_element_matrices(c, 0.3)
+        if mesh.kind == "hex":
+            c = mesh.p[:, mesh.t[:, 0]]
+            _, self.Kloc = fem.hex_element_matrices(c, 0.3)
+        else:
+            _, self.Kloc, _ = fem.element_matrices(mesh, 0.3)
         self.dofs = fem.element_dofs(mesh.t, 1)
         self.h = robin_coefficient
         self.t_env = robin_bc_value
@@ -256,7 +314,7 @@ class HeatRobinProblem:
         self.q = float(q)
         self.pairing = pairing
         self.emit = np.zeros(mesh.nnodes) if emit is None else np.asarray(emit, float)
-        self.Q = hex_quadrature(mesh)
+        self.Q = element_quadrature(mesh)
         # surface Robin terms (rho independent)
         self.surf_K = sp.csr_matrix((mesh.nnodes, mesh.nnodes))
         self.surf_f = np.zeros(mesh.nnodes)
@@ -267,7 +325,8 @@ class HeatRobinProblem:
             for faces, hh, tt in zip(groups, hs, ts):
                 Me, load = surface_robin(mesh, np.asarray(faces), hh, tt)
                 if len(faces):
-                    sub = np.zeros((mesh.nelements, 8, 8))
+                    nloc = mesh.t.shape[0]
+                    sub = np.zeros((mesh.nelements, nloc, nloc))
                     np.add.at(sub, np.asarray(faces)[:, 0], Me)
                     self.surf_K = self.surf_K + _assemble_mats(mesh, sub)
                 self.surf_f += load

@@ -1,14 +1,17 @@
-// Heat plugin on hexahedral meshes: the density-dependent ("virtual") and
-// surface Robin terms, the heat-exchange objective and its adjoint load, the
-// explicit Robin gradient of the compliance objective and the per-element
-// grad T . grad lam products of FEM_SimpLinearHeatConduction
+// Heat plugin on hexahedral and P1 tetrahedral meshes: the density-dependent
+// ("virtual") and surface Robin terms, the heat-exchange objective and its
+// adjoint load, the explicit Robin gradient of the compliance objective and
+// the per-element grad T . grad lam products of FEM_SimpLinearHeatConduction
 // (sktopt/fea/solver_heat.py:306-625, 705-980).
 //
-// Every volume integral uses the 2x2x2 Gauss rule of the element matrices on
-// axis-aligned hexahedra (MeshHex local node order).  Nodal sums run over a
-// node -> (a, e) list kept in t.ravel() order (t is 8 x n_elem), so they are
-// deterministic, and the nodal density average adds in exactly the order of
-// the reference's np.add.at.
+// Every volume integral uses the quadrature of a basis with intorder 2: the
+// 2x2x2 Gauss rule on axis-aligned hexahedra (MeshHex local node order), the
+// 4-point degree-2 rule on tetrahedra (barycentric points (a, b, b, b),
+// a = (5 + 3 sqrt 5) / 20, b = (5 - sqrt 5) / 20, weights V / 4; the P1
+// gradients are constant per element and precomputed).  Nodal sums run over
+// a node -> (a, e) list kept in t.ravel() order (t is nloc x n_elem), so
+// they are deterministic, and the nodal density average adds in exactly the
+// order of the reference's np.add.at.
 
 #include <algorithm>
 #include <cmath>
@@ -32,9 +35,11 @@ __host__ __device__ constexpr int hex_off(int a, int d) { return (0xF73850 >> (3
 
 // Shape values and physical gradients of the trilinear hexahedron with
 // extents (hx, hy, hz) at Gauss point q (bits: x, y, z coordinate index).
-struct Qp {
-  double N[8], gx[8], gy[8], gz[8];
+template <int NL>
+struct QpT {
+  double N[NL], gx[NL], gy[NL], gz[NL];
 };
+using Qp = QpT<8>;
 __device__ __forceinline__ void qpoint(int q, double G, double hx, double hy, double hz,
                                        Qp& o) {
   const double x = (q >> 2) & 1 ? 0.5 + G : 0.5 - G;
@@ -58,30 +63,72 @@ __device__ __forceinline__ void qpoint(int q, double G, double hx, double hy, do
 __device__ __forceinline__ double gauss_offset() { return 0.5 / sqrt(3.0); }
 
 struct Geo {
-  const int32_t* t;     // 8 x ne
-  const double* hsz;    // 3 x ne
+  const int32_t* t;     // nloc x ne
+  const double* hsz;    // hexahedra: 3 x ne extents
+  const double* tg;     // tetrahedra: ne x 4 x 3 shape-function gradients
+  const double* tv;     // tetrahedra: ne volumes
   int64_t ne;
 };
 
-__device__ __forceinline__ void load_elem(const Geo& g, int64_t e, const double* x, double (&v)[8],
-                                          int64_t (&node)[8], double& hx, double& hy,
-                                          double& hz) {
+// Geometry of one element: hexahedron extents or tetrahedron gradients, and
+// the quadrature weight w (times detJ) shared by its points.
+template <int NL>
+struct ElemG {
+  double hx, hy, hz, w;
+  double g[NL][3];
+};
+
+template <int NL>
+__device__ __forceinline__ void load_elem(const Geo& g, int64_t e, const double* x,
+                                          double (&v)[NL], int64_t (&node)[NL], ElemG<NL>& E) {
 #pragma unroll
-  for (int a = 0; a < 8; ++a) {
+  for (int a = 0; a < NL; ++a) {
     node[a] = g.t[(int64_t)a * g.ne + e];
     v[a] = x ? x[node[a]] : 0.0;
   }
-  hx = g.hsz[e];
-  hy = g.hsz[g.ne + e];
-  hz = g.hsz[2 * g.ne + e];
+  if (NL == 8) {
+    E.hx = g.hsz[e];
+    E.hy = g.hsz[g.ne + e];
+    E.hz = g.hsz[2 * g.ne + e];
+    E.w = 0.125 * (E.hx * E.hy * E.hz);
+  } else {
+#pragma unroll
+    for (int a = 0; a < NL; ++a)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) E.g[a][d] = g.tg[e * 12 + a * 3 + d];
+    E.w = 0.25 * g.tv[e];
+  }
+}
+
+// Quadrature points of an element: 8 Gauss points of the hexahedron, 4
+// points of the tetrahedron rule.
+template <int NL>
+__host__ __device__ constexpr int n_qp() { return NL == 8 ? 8 : 4; }
+
+template <int NL>
+__device__ __forceinline__ void elem_qp(int qi, const ElemG<NL>& E, QpT<NL>& Q) {
+  if constexpr (NL == 8) {
+    qpoint(qi, gauss_offset(), E.hx, E.hy, E.hz, Q);
+  } else {
+    const double ta = 0.58541019662496845446, tb = 0.13819660112501051518;
+#pragma unroll
+    for (int a = 0; a < NL; ++a) {
+      Q.N[a] = a == qi ? ta : tb;
+      Q.gx[a] = E.g[a][0];
+      Q.gy[a] = E.g[a][1];
+      Q.gz[a] = E.g[a][2];
+    }
+  }
 }
 
 // rho_node[n] = sum over the (a, e) of node n, in t.ravel() order, of
-// rho[src] / max(count, 1), src = (a ne + e) / 8 (pairing 0: np.repeat(rho,
-// 8) against t.ravel(), solver_heat.py:600-613) or e (pairing 1).
+// rho[src] / max(count, 1), src = (a ne + e) / nloc (pairing 0:
+// np.repeat(rho, nloc) against t.ravel(), solver_heat.py:600-613) or e
+// (pairing 1).
 __global__ void k_nodal_average(int64_t nn, const int32_t* __restrict__ ptr,
-                                const int32_t* __restrict__ adj, int64_t ne, int pairing,
-                                const double* __restrict__ rho, double* __restrict__ out) {
+                                const int32_t* __restrict__ adj, int64_t ne, int nloc,
+                                int pairing, const double* __restrict__ rho,
+                                double* __restrict__ out) {
   TOPT_KERNEL_COUNT();
   for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nn;
        n += (int64_t)gridDim.x * blockDim.x) {
@@ -89,7 +136,7 @@ __global__ void k_nodal_average(int64_t nn, const int32_t* __restrict__ ptr,
     double s = 0.0;
     for (int32_t k = k0; k < k1; ++k) {
       const int64_t idx = adj[k];
-      s += rho[pairing == 0 ? idx / 8 : idx % ne];
+      s += rho[pairing == 0 ? idx / nloc : idx % ne];
     }
     const double c = (double)(k1 - k0);
     out[n] = s / (c > 1.0 ? c : 1.0);
@@ -98,35 +145,35 @@ __global__ void k_nodal_average(int64_t nn, const int32_t* __restrict__ ptr,
 
 // Virtual Robin element matrices and loads (get_robin_virtual,
 // solver_heat.py:552-572): c = w detJ h rho^p (1 - rho)^q |grad rho| at every
-// Gauss point, M_ab += c N_a N_b, f_a += c T_env N_a; plus the element's
+// quadrature point, M_ab += c N_a N_b, f_a += c T_env N_a; plus the element's
 // surface Robin matrix (task_heat.py:60-139) when it has Robin facets.
+template <int NL>
 __global__ void k_robin_elem(Geo g, const double* __restrict__ rho_n, double h, double t_env,
                              double p, double q, int virt, const int32_t* __restrict__ surf_idx,
                              const double* __restrict__ surf, double* __restrict__ extra,
                              double* __restrict__ fe) {
   TOPT_KERNEL_COUNT();
-  const double G = gauss_offset();
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double M[8][8], f[8];
+    double M[NL][NL], f[NL];
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
+    for (int a = 0; a < NL; ++a) {
       f[a] = 0.0;
 #pragma unroll
-      for (int b = 0; b < 8; ++b) M[a][b] = 0.0;
+      for (int b = 0; b < NL; ++b) M[a][b] = 0.0;
     }
     if (virt) {
-      double r[8], hx, hy, hz;
-      int64_t node[8];
-      load_elem(g, e, rho_n, r, node, hx, hy, hz);
-      const double w = 0.125 * (hx * hy * hz);
+      double r[NL];
+      int64_t node[NL];
+      ElemG<NL> E;
+      load_elem<NL>(g, e, rho_n, r, node, E);
 #pragma unroll 1
-      for (int qi = 0; qi < 8; ++qi) {
-        Qp Q;
-        qpoint(qi, G, hx, hy, hz, Q);
+      for (int qi = 0; qi < n_qp<NL>(); ++qi) {
+        QpT<NL> Q;
+        elem_qp<NL>(qi, E, Q);
         double rq = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
+        for (int a = 0; a < NL; ++a) {
           rq += Q.N[a] * r[a];
           gx += Q.gx[a] * r[a];
           gy += Q.gy[a] * r[a];
@@ -134,37 +181,37 @@ __global__ void k_robin_elem(Geo g, const double* __restrict__ rho_n, double h, 
         }
         const double iface = sqrt(gx * gx + gy * gy + gz * gz);
         const double heff = h * pow(rq, p) * pow(1.0 - rq, q);
-        const double c = w * heff * iface;
+        const double c = E.w * heff * iface;
         const double ct = c * t_env;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
+        for (int a = 0; a < NL; ++a) {
           f[a] += ct * Q.N[a];
           const double ca = c * Q.N[a];
 #pragma unroll
-          for (int b = a; b < 8; ++b) M[a][b] += ca * Q.N[b];
+          for (int b = a; b < NL; ++b) M[a][b] += ca * Q.N[b];
         }
       }
     }
     const int32_t si = surf_idx ? surf_idx[e] : -1;
-    double* X = extra + e * 64;
+    double* X = extra + e * NL * NL;
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < NL; ++a)
 #pragma unroll
-      for (int b = 0; b < 8; ++b) {
+      for (int b = 0; b < NL; ++b) {
         double v = a <= b ? M[a][b] : M[b][a];
-        if (si >= 0) v += surf[(int64_t)si * 64 + a * 8 + b];
-        X[a * 8 + b] = v;
+        if (si >= 0) v += surf[(int64_t)si * NL * NL + a * NL + b];
+        X[a * NL + b] = v;
       }
     if (fe) {
 #pragma unroll
-      for (int a = 0; a < 8; ++a) fe[e * 8 + a] = f[a];
+      for (int a = 0; a < NL; ++a) fe[e * NL + a] = f[a];
     }
   }
 }
 
 // out[n] = (sum over the (a, e) of node n of fe[e][a]) / div.
 __global__ void k_node_gather(int64_t nn, const int32_t* __restrict__ ptr,
-                              const int32_t* __restrict__ adj, int64_t ne,
+                              const int32_t* __restrict__ adj, int64_t ne, int nloc,
                               const double* __restrict__ fe, double div,
                               double* __restrict__ out) {
   TOPT_KERNEL_COUNT();
@@ -174,7 +221,7 @@ __global__ void k_node_gather(int64_t nn, const int32_t* __restrict__ ptr,
     for (int32_t k = ptr[n]; k < ptr[n + 1]; ++k) {
       const int64_t idx = adj[k];
       const int64_t a = idx / ne, e = idx - a * ne;
-      s += fe[e * 8 + a];
+      s += fe[e * nloc + a];
     }
     out[n] = div == 1.0 ? s : s / div;
   }
@@ -183,45 +230,45 @@ __global__ void k_node_gather(int64_t nn, const int32_t* __restrict__ ptr,
 // Heat-exchange integrals (solver_heat.py:306-321, 382-390): den = sum of
 // w detJ |grad rho|, num_j = sum of w detJ (-T_env h (T_j - T_env) |grad rho|)
 // for L <= 4 temperature columns (T: n_nodes x L row-major).
+template <int NL>
 __global__ void __launch_bounds__(kHB)
 k_hx_reduce(Geo g, const double* __restrict__ rho_n, const double* __restrict__ T, int L,
             double h, double t_env, double* __restrict__ partials, unsigned* __restrict__ counter,
             double* __restrict__ out) {
   TOPT_KERNEL_COUNT();
-  const double G = gauss_offset();
   double v[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double r[8], hx, hy, hz;
-    int64_t node[8];
-    load_elem(g, e, rho_n, r, node, hx, hy, hz);
-    double te[4][8];
+    double r[NL];
+    int64_t node[NL];
+    ElemG<NL> E;
+    load_elem<NL>(g, e, rho_n, r, node, E);
+    double te[4][NL];
 #pragma unroll
     for (int j = 0; j < 4; ++j)
 #pragma unroll
-      for (int a = 0; a < 8; ++a) te[j][a] = j < L ? T[node[a] * L + j] : 0.0;
-    const double w = 0.125 * (hx * hy * hz);
+      for (int a = 0; a < NL; ++a) te[j][a] = j < L ? T[node[a] * L + j] : 0.0;
     double den = 0.0, num[4] = {0.0, 0.0, 0.0, 0.0};
 #pragma unroll 1
-    for (int qi = 0; qi < 8; ++qi) {
-      Qp Q;
-      qpoint(qi, G, hx, hy, hz, Q);
+    for (int qi = 0; qi < n_qp<NL>(); ++qi) {
+      QpT<NL> Q;
+      elem_qp<NL>(qi, E, Q);
       double gx = 0.0, gy = 0.0, gz = 0.0;
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
+      for (int a = 0; a < NL; ++a) {
         gx += Q.gx[a] * r[a];
         gy += Q.gy[a] * r[a];
         gz += Q.gz[a] * r[a];
       }
       const double iface = sqrt(gx * gx + gy * gy + gz * gz);
-      den += w * iface;
+      den += E.w * iface;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (j < L) {
           double tq = 0.0;
 #pragma unroll
-          for (int a = 0; a < 8; ++a) tq += Q.N[a] * te[j][a];
-          num[j] += w * (-t_env * h * (tq - t_env) * iface);
+          for (int a = 0; a < NL; ++a) tq += Q.N[a] * te[j][a];
+          num[j] += E.w * (-t_env * h * (tq - t_env) * iface);
         }
       }
     }
@@ -237,37 +284,39 @@ k_hx_reduce(Geo g, const double* __restrict__ rho_n, const double* __restrict__ 
 // Element loads of the heat-exchange adjoint (_hx_adj_rhs_,
 // solver_heat.py:392-408): h_eff the interpolated nodal h rho^p (1 - rho)^q
 // (825-830), f_a += w detJ (-T_env h_eff |grad rho|) N_a.
+template <int NL>
 __global__ void k_hx_adj_elem(Geo g, const double* __restrict__ rho_n, double h, double t_env,
                               double p, double q, double* __restrict__ fe) {
   TOPT_KERNEL_COUNT();
-  const double G = gauss_offset();
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double r[8], hn[8], hx, hy, hz;
-    int64_t node[8];
-    load_elem(g, e, rho_n, r, node, hx, hy, hz);
+    double r[NL], hn[NL];
+    int64_t node[NL];
+    ElemG<NL> E;
+    load_elem<NL>(g, e, rho_n, r, node, E);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) hn[a] = h * pow(r[a], p) * pow(1.0 - r[a], q);
-    const double w = 0.125 * (hx * hy * hz);
-    double f[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int a = 0; a < NL; ++a) hn[a] = h * pow(r[a], p) * pow(1.0 - r[a], q);
+    double f[NL];
+#pragma unroll
+    for (int a = 0; a < NL; ++a) f[a] = 0.0;
 #pragma unroll 1
-    for (int qi = 0; qi < 8; ++qi) {
-      Qp Q;
-      qpoint(qi, G, hx, hy, hz, Q);
+    for (int qi = 0; qi < n_qp<NL>(); ++qi) {
+      QpT<NL> Q;
+      elem_qp<NL>(qi, E, Q);
       double hq = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
+      for (int a = 0; a < NL; ++a) {
         hq += Q.N[a] * hn[a];
         gx += Q.gx[a] * r[a];
         gy += Q.gy[a] * r[a];
         gz += Q.gz[a] * r[a];
       }
-      const double c = w * (-t_env * hq * sqrt(gx * gx + gy * gy + gz * gz));
+      const double c = E.w * (-t_env * hq * sqrt(gx * gx + gy * gy + gz * gz));
 #pragma unroll
-      for (int a = 0; a < 8; ++a) f[a] += c * Q.N[a];
+      for (int a = 0; a < NL; ++a) f[a] += c * Q.N[a];
     }
 #pragma unroll
-    for (int a = 0; a < 8; ++a) fe[e * 8 + a] = f[a];
+    for (int a = 0; a < NL; ++a) fe[e * NL + a] = f[a];
   }
 }
 
@@ -276,27 +325,29 @@ __global__ void k_hx_adj_elem(Geo g, const double* __restrict__ rho_n, double h,
 // da, phi = 2 T_env T - T^2,
 //   f_a += w detJ h (da |grad rho| phi N_a + a phi (grad rho / max(|grad rho|,
 //   1e-12)) . grad N_a).
+template <int NL>
 __global__ void k_robin_grad_elem(Geo g, const double* __restrict__ rho_n,
                                   const double* __restrict__ T, int L, int j, double h,
                                   double t_env, double p, double q, double* __restrict__ fe) {
   TOPT_KERNEL_COUNT();
-  const double G = gauss_offset();
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double r[8], te[8], hx, hy, hz;
-    int64_t node[8];
-    load_elem(g, e, rho_n, r, node, hx, hy, hz);
+    double r[NL], te[NL];
+    int64_t node[NL];
+    ElemG<NL> E;
+    load_elem<NL>(g, e, rho_n, r, node, E);
 #pragma unroll
-    for (int a = 0; a < 8; ++a) te[a] = T[node[a] * L + j];
-    const double w = 0.125 * (hx * hy * hz);
-    double f[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int a = 0; a < NL; ++a) te[a] = T[node[a] * L + j];
+    double f[NL];
+#pragma unroll
+    for (int a = 0; a < NL; ++a) f[a] = 0.0;
 #pragma unroll 1
-    for (int qi = 0; qi < 8; ++qi) {
-      Qp Q;
-      qpoint(qi, G, hx, hy, hz, Q);
+    for (int qi = 0; qi < n_qp<NL>(); ++qi) {
+      QpT<NL> Q;
+      elem_qp<NL>(qi, E, Q);
       double rq = 0.0, tq = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
+      for (int a = 0; a < NL; ++a) {
         rq += Q.N[a] * r[a];
         tq += Q.N[a] * te[a];
         gx += Q.gx[a] * r[a];
@@ -309,20 +360,21 @@ __global__ void k_robin_grad_elem(Geo g, const double* __restrict__ rho_n,
       const double av = rp * sq;
       const double da = p * pow(rq, p - 1.0) * sq - q * rp * pow(1.0 - rq, q - 1.0);
       const double phi = 2.0 * t_env * tq - tq * tq;
-      const double c1 = w * h * da * iface * phi;
-      const double c2 = w * h * av * phi;
+      const double c1 = E.w * h * da * iface * phi;
+      const double c2 = E.w * h * av * phi;
       const double nx = gx / safe, ny = gy / safe, nz = gz / safe;
 #pragma unroll
-      for (int a = 0; a < 8; ++a)
+      for (int a = 0; a < NL; ++a)
         f[a] += c1 * Q.N[a] + c2 * (nx * Q.gx[a] + ny * Q.gy[a] + nz * Q.gz[a]);
     }
 #pragma unroll
-    for (int a = 0; a < 8; ++a) fe[e * 8 + a] = f[a];
+    for (int a = 0; a < NL; ++a) fe[e * NL + a] = f[a];
   }
 }
 
 // _nodal_gradient_to_element_gradient (solver_heat.py:616-625), added to
 // column j: grad[e][j] += sum_a nodal[t[a][e]] / max(count, 1).
+template <int NL>
 __global__ void k_nodal_to_elem(Geo g, const int32_t* __restrict__ ptr,
                                 const double* __restrict__ nodal, int L, int j,
                                 double* __restrict__ grad) {
@@ -331,7 +383,7 @@ __global__ void k_nodal_to_elem(Geo g, const int32_t* __restrict__ ptr,
        e += (int64_t)gridDim.x * blockDim.x) {
     double s = 0.0;
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
+    for (int a = 0; a < NL; ++a) {
       const int64_t n = g.t[(int64_t)a * g.ne + e];
       const double c = (double)(ptr[n + 1] - ptr[n]);
       s += nodal[n] / (c > 1.0 ? c : 1.0);
@@ -342,38 +394,38 @@ __global__ void k_nodal_to_elem(Geo g, const int32_t* __restrict__ ptr,
 
 // out[e][j] = integral over e of grad X_j . grad Y_j (solver_heat.py:324-379,
 // 529-550).  X, Y: n_nodes x L row-major.
+template <int NL>
 __global__ void k_grad_dot(Geo g, const double* __restrict__ X, const double* __restrict__ Y,
                            int L, double* __restrict__ out) {
   TOPT_KERNEL_COUNT();
-  const double G = gauss_offset();
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < g.ne;
        e += (int64_t)gridDim.x * blockDim.x) {
-    double hx, hy, hz, dummy[8];
-    int64_t node[8];
-    load_elem(g, e, nullptr, dummy, node, hx, hy, hz);
-    const double w = 0.125 * (hx * hy * hz);
+    double dummy[NL];
+    int64_t node[NL];
+    ElemG<NL> E;
+    load_elem<NL>(g, e, nullptr, dummy, node, E);
     for (int j = 0; j < L; ++j) {
       // shifted by the node-0 values: gradients of large offset fields
       // (prescribed temperatures) without cancellation
-      double xe[8], ye[8];
+      double xe[NL], ye[NL];
       const double x0 = X[node[0] * L + j], y0 = Y[node[0] * L + j];
 #pragma unroll
-      for (int a = 0; a < 8; ++a) {
+      for (int a = 0; a < NL; ++a) {
         xe[a] = X[node[a] * L + j] - x0;
         ye[a] = Y[node[a] * L + j] - y0;
       }
       double s = 0.0;
 #pragma unroll 1
-      for (int qi = 0; qi < 8; ++qi) {
-        Qp Q;
-        qpoint(qi, G, hx, hy, hz, Q);
+      for (int qi = 0; qi < n_qp<NL>(); ++qi) {
+        QpT<NL> Q;
+        elem_qp<NL>(qi, E, Q);
         double ax = 0.0, ay = 0.0, az = 0.0, bx = 0.0, by = 0.0, bz = 0.0;
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
+        for (int a = 0; a < NL; ++a) {
           ax += Q.gx[a] * xe[a]; ay += Q.gy[a] * xe[a]; az += Q.gz[a] * xe[a];
           bx += Q.gx[a] * ye[a]; by += Q.gy[a] * ye[a]; bz += Q.gz[a] * ye[a];
         }
-        s += w * (ax * bx + ay * by + az * bz);
+        s += E.w * (ax * bx + ay * by + az * bz);
       }
       out[e * L + j] = s;
     }
@@ -391,70 +443,128 @@ int launches_heat(unsigned long long* out) {
 
 struct topt_heat {
   int64_t n_nodes = 0, n_elem = 0;
+  int nloc = 8;
   int pairing = 0;
   int sm = 152;
   cudaStream_t stream = nullptr;
-  DevBuf t, hsz, node_ptr, adj;
+  DevBuf t, hsz, tg, tv, node_ptr, adj;
   DevBuf surf_idx, surf;
   DevBuf fe, nodal;                   // element-vector and nodal scratch
   DevBuf partials, counter, out;      // k_hx_reduce
   int red_blocks = 0;
-  topt::Geo geo() const { return {t.as<int32_t>(), hsz.as<double>(), n_elem}; }
+  topt::Geo geo() const {
+    return {t.as<int32_t>(), hsz.as<double>(), tg.as<double>(), tv.as<double>(), n_elem};
+  }
   int grid(int64_t n) const { return topt::grid_for(n, topt::kHB, sm * 16); }
 };
 
+#define TOPT_HEAT_NL(h, CALL)                      \
+  do {                                             \
+    if ((h)->nloc == 8) { constexpr int NL_ = 8; CALL; } \
+    else { constexpr int NL_ = 4; CALL; }          \
+  } while (0)
+
 extern "C" {
 
-int topt_heat_create(int64_t n_nodes, int64_t n_elem, const int32_t* t, const double* p,
-                     int32_t pairing, topt_heat** out) {
+int topt_heat_create_mesh(int64_t n_nodes, int64_t n_elem, int32_t nloc, const int32_t* t,
+                          const double* p, int32_t pairing, topt_heat** out) {
   using namespace topt;
-  if (!out || !t || !p || n_nodes <= 0 || n_elem <= 0 || (pairing != 0 && pairing != 1))
+  if (!out || !t || !p || n_nodes <= 0 || n_elem <= 0 || (pairing != 0 && pairing != 1) ||
+      (nloc != 8 && nloc != 4))
     return fail(TOPT_BAD_INPUT, "heat_create: bad argument");
-  if (n_elem * 8 >= (int64_t)INT32_MAX || n_nodes >= (int64_t)INT32_MAX)
+  if (n_elem * nloc >= (int64_t)INT32_MAX || n_nodes >= (int64_t)INT32_MAX)
     return fail(TOPT_BAD_INPUT, "heat_create: mesh too large for 32-bit indices");
   *out = nullptr;
-  // extents of every cell; the Robin kernels need axis-aligned boxes
-  std::vector<double> hs(3 * (size_t)n_elem);
-  for (int64_t e = 0; e < n_elem; ++e) {
-    int64_t nd[8];
-    for (int a = 0; a < 8; ++a) {
-      nd[a] = t[(int64_t)a * n_elem + e];
-      if (nd[a] < 0 || nd[a] >= n_nodes) return fail(TOPT_BAD_INPUT, "heat_create: bad node index");
-    }
-    double lo[3], ext[3];
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = p[d * n_nodes + nd[0]];
-      ext[d] = p[d * n_nodes + nd[7]] - lo[d];
-      if (!(ext[d] > 0.0)) return fail(TOPT_BAD_INPUT, "heat_create: cell with non-positive extent");
-      hs[(size_t)d * n_elem + e] = ext[d];
-    }
-    for (int a = 0; a < 8; ++a)
+  for (int64_t i = 0; i < (int64_t)nloc * n_elem; ++i)
+    if (t[i] < 0 || t[i] >= n_nodes) return fail(TOPT_BAD_INPUT, "heat_create: bad node index");
+  std::vector<double> hs, tg, tv;
+  if (nloc == 8) {
+    // extents of every cell; the Robin kernels need axis-aligned boxes
+    hs.resize(3 * (size_t)n_elem);
+    for (int64_t e = 0; e < n_elem; ++e) {
+      int64_t nd[8];
+      for (int a = 0; a < 8; ++a) nd[a] = t[(int64_t)a * n_elem + e];
+      double lo[3], ext[3];
       for (int d = 0; d < 3; ++d) {
-        const double want = lo[d] + (hex_off(a, d) ? ext[d] : 0.0);
-        if (std::fabs(p[d * n_nodes + nd[a]] - want) > 1e-9 * ext[d])
-          return fail(TOPT_BAD_INPUT, "heat_create: cells must be axis-aligned boxes");
+        lo[d] = p[d * n_nodes + nd[0]];
+        ext[d] = p[d * n_nodes + nd[7]] - lo[d];
+        if (!(ext[d] > 0.0))
+          return fail(TOPT_BAD_INPUT, "heat_create: cell with non-positive extent");
+        hs[(size_t)d * n_elem + e] = ext[d];
       }
+      for (int a = 0; a < 8; ++a)
+        for (int d = 0; d < 3; ++d) {
+          const double want = lo[d] + (hex_off(a, d) ? ext[d] : 0.0);
+          if (std::fabs(p[d * n_nodes + nd[a]] - want) > 1e-9 * ext[d])
+            return fail(TOPT_BAD_INPUT, "heat_create: cells must be axis-aligned boxes");
+        }
+    }
+  } else {
+    // P1 gradients: with J the columns x1 - x0, x2 - x0, x3 - x0, the
+    // reference gradients (-1,-1,-1), e1, e2, e3 map by J^-T; volume |det J|/6
+    tg.resize(12 * (size_t)n_elem);
+    tv.resize((size_t)n_elem);
+    for (int64_t e = 0; e < n_elem; ++e) {
+      double x[4][3];
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) x[a][d] = p[d * n_nodes + t[(int64_t)a * n_elem + e]];
+      double J[3][3];
+      for (int d = 0; d < 3; ++d)
+        for (int k = 0; k < 3; ++k) J[d][k] = x[k + 1][d] - x[0][d];
+      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+      const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+      const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+      const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      if (!(std::fabs(det) > 0.0)) return fail(TOPT_BAD_INPUT, "heat_create: degenerate tetrahedron");
+      // inverse of J (rows: d xi_k / d x_d transposed as Jinv[k][d])
+      double Ji[3][3];
+      Ji[0][0] = c00 / det;
+      Ji[1][0] = c01 / det;
+      Ji[2][0] = c02 / det;
+      Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+      Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+      Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+      Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+      Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+      Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+      // dN_a/dx_d = sum_k dN_a/dxi_k Jinv[k][d]
+      const double gr[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+      for (int a = 0; a < 4; ++a)
+        for (int d = 0; d < 3; ++d) {
+          double v = 0.0;
+          for (int k = 0; k < 3; ++k) v += gr[a][k] * Ji[k][d];
+          tg[(size_t)e * 12 + a * 3 + d] = v;
+        }
+      tv[e] = std::fabs(det) / 6.0;
+    }
   }
   // node -> raveled (a, e) list in t.ravel() order
-  std::vector<int32_t> ptr(n_nodes + 1, 0), adj(8 * (size_t)n_elem);
-  for (int64_t i = 0; i < 8 * n_elem; ++i) ptr[t[i] + 1]++;
+  const int64_t nt = (int64_t)nloc * n_elem;
+  std::vector<int32_t> ptr(n_nodes + 1, 0), adj((size_t)nt);
+  for (int64_t i = 0; i < nt; ++i) ptr[t[i] + 1]++;
   for (int64_t n = 0; n < n_nodes; ++n) ptr[n + 1] += ptr[n];
   {
     std::vector<int32_t> pos(ptr.begin(), ptr.end() - 1);
-    for (int64_t i = 0; i < 8 * n_elem; ++i) adj[pos[t[i]]++] = (int32_t)i;
+    for (int64_t i = 0; i < nt; ++i) adj[pos[t[i]]++] = (int32_t)i;
   }
   std::unique_ptr<topt_heat> h(new topt_heat());
   h->n_nodes = n_nodes;
   h->n_elem = n_elem;
+  h->nloc = nloc;
   h->pairing = pairing;
   h->sm = device_sm_count();
   int rc;
   cudaStream_t s = nullptr;
-  if ((rc = upload(h->t, t, 8 * (size_t)n_elem, s))) return rc;
-  if ((rc = upload(h->hsz, hs.data(), hs.size(), s))) return rc;
+  if ((rc = upload(h->t, t, (size_t)nt, s))) return rc;
+  if (nloc == 8) {
+    if ((rc = upload(h->hsz, hs.data(), hs.size(), s))) return rc;
+  } else {
+    if ((rc = upload(h->tg, tg.data(), tg.size(), s))) return rc;
+    if ((rc = upload(h->tv, tv.data(), tv.size(), s))) return rc;
+  }
   if ((rc = upload(h->node_ptr, ptr.data(), ptr.size(), s))) return rc;
   if ((rc = upload(h->adj, adj.data(), adj.size(), s))) return rc;
-  if ((rc = h->fe.alloc(sizeof(double) * 8 * (size_t)n_elem))) return rc;
+  if ((rc = h->fe.alloc(sizeof(double) * (size_t)nt))) return rc;
   if ((rc = h->nodal.alloc(sizeof(double) * (size_t)n_nodes))) return rc;
   h->red_blocks = h->grid(n_elem);
   if ((rc = h->partials.alloc(sizeof(double) * 5 * (size_t)h->red_blocks))) return rc;
@@ -464,6 +574,11 @@ int topt_heat_create(int64_t n_nodes, int64_t n_elem, const int32_t* t, const do
   TOPT_CUDA(cudaDeviceSynchronize());
   *out = h.release();
   return TOPT_OK;
+}
+
+int topt_heat_create(int64_t n_nodes, int64_t n_elem, const int32_t* t, const double* p,
+                     int32_t pairing, topt_heat** out) {
+  return topt_heat_create_mesh(n_nodes, n_elem, 8, t, p, pairing, out);
 }
 
 void topt_heat_destroy(topt_heat* h) { delete h; }
@@ -479,17 +594,18 @@ int topt_heat_set_surface(topt_heat* h, int64_t n_faces, const int32_t* elems,
   using namespace topt;
   if (!h || n_faces < 0 || (n_faces > 0 && (!elems || !mats)))
     return fail(TOPT_BAD_INPUT, "heat_set_surface: bad argument");
+  const int nn = h->nloc * h->nloc;
   std::vector<int32_t> idx(h->n_elem, -1);
   std::vector<double> m;
   for (int64_t k = 0; k < n_faces; ++k) {
     const int32_t e = elems[k];
     if (e < 0 || e >= h->n_elem) return fail(TOPT_BAD_INPUT, "heat_set_surface: bad element");
     if (idx[e] < 0) {
-      idx[e] = (int32_t)(m.size() / 64);
-      m.resize(m.size() + 64, 0.0);
+      idx[e] = (int32_t)(m.size() / nn);
+      m.resize(m.size() + nn, 0.0);
     }
-    double* dst = m.data() + (size_t)idx[e] * 64;
-    for (int i = 0; i < 64; ++i) dst[i] += mats[k * 64 + i];
+    double* dst = m.data() + (size_t)idx[e] * nn;
+    for (int i = 0; i < nn; ++i) dst[i] += mats[k * nn + i];
   }
   int rc;
   if (m.empty()) {
@@ -507,8 +623,8 @@ int topt_heat_nodal_average(topt_heat* h, const double* rho, double* rho_node) {
   using namespace topt;
   if (!h || !rho || !rho_node) return fail(TOPT_BAD_INPUT, "heat_nodal_average: null argument");
   k_nodal_average<<<h->grid(h->n_nodes), kHB, 0, h->stream>>>(
-      h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem, h->pairing, rho,
-      rho_node);
+      h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem, h->nloc,
+      h->pairing, rho, rho_node);
   TOPT_CHECK_LAUNCH("k_nodal_average");
   return TOPT_OK;
 }
@@ -518,13 +634,14 @@ int topt_heat_robin(topt_heat* h, const double* rho_node, double h_coef, double 
   using namespace topt;
   if (!h || !extra || (virtual_on && !rho_node))
     return fail(TOPT_BAD_INPUT, "heat_robin: null argument");
-  k_robin_elem<<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
-      h->geo(), rho_node, h_coef, t_env, p, q, virtual_on ? 1 : 0, h->surf_idx.as<int32_t>(),
-      h->surf.as<double>(), extra, load ? h->fe.as<double>() : nullptr);
+  TOPT_HEAT_NL(h, (k_robin_elem<NL_><<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
+                      h->geo(), rho_node, h_coef, t_env, p, q, virtual_on ? 1 : 0,
+                      h->surf_idx.as<int32_t>(), h->surf.as<double>(), extra,
+                      load ? h->fe.as<double>() : nullptr)));
   TOPT_CHECK_LAUNCH("k_robin_elem");
   if (load) {
     k_node_gather<<<h->grid(h->n_nodes), kHB, 0, h->stream>>>(
-        h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem,
+        h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem, h->nloc,
         h->fe.as<double>(), 1.0, load);
     TOPT_CHECK_LAUNCH("k_node_gather");
   }
@@ -536,9 +653,9 @@ int topt_heat_exchange(topt_heat* h, const double* rho_node, const double* T, in
   using namespace topt;
   if (!h || !rho_node || !den || L < 0 || L > 4 || (L > 0 && (!T || !num)))
     return fail(TOPT_BAD_INPUT, "heat_exchange: bad argument");
-  k_hx_reduce<<<h->red_blocks, kHB, 0, h->stream>>>(
-      h->geo(), rho_node, T, L, h_coef, t_env, h->partials.as<double>(),
-      h->counter.as<unsigned>(), h->out.as<double>());
+  TOPT_HEAT_NL(h, (k_hx_reduce<NL_><<<h->red_blocks, kHB, 0, h->stream>>>(
+                      h->geo(), rho_node, T, L, h_coef, t_env, h->partials.as<double>(),
+                      h->counter.as<unsigned>(), h->out.as<double>())));
   TOPT_CHECK_LAUNCH("k_hx_reduce");
   double r[5];
   TOPT_CUDA(cudaMemcpyAsync(r, h->out.p, sizeof(r), cudaMemcpyDeviceToHost, h->stream));
@@ -553,11 +670,11 @@ int topt_heat_exchange_adjoint(topt_heat* h, const double* rho_node, double h_co
   using namespace topt;
   if (!h || !rho_node || !rhs || !(den > 0.0))
     return fail(TOPT_BAD_INPUT, "heat_exchange_adjoint: bad argument");
-  k_hx_adj_elem<<<h->grid(h->n_elem), kHB, 0, h->stream>>>(h->geo(), rho_node, h_coef, t_env,
-                                                            p, q, h->fe.as<double>());
+  TOPT_HEAT_NL(h, (k_hx_adj_elem<NL_><<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
+                      h->geo(), rho_node, h_coef, t_env, p, q, h->fe.as<double>())));
   TOPT_CHECK_LAUNCH("k_hx_adj_elem");
   k_node_gather<<<h->grid(h->n_nodes), kHB, 0, h->stream>>>(
-      h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem,
+      h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem, h->nloc,
       h->fe.as<double>(), den, rhs);
   TOPT_CHECK_LAUNCH("k_node_gather");
   return TOPT_OK;
@@ -569,15 +686,16 @@ int topt_heat_robin_grad(topt_heat* h, const double* rho_node, const double* T, 
   if (!h || !rho_node || !T || !grad || L < 1 || L > 64)
     return fail(TOPT_BAD_INPUT, "heat_robin_grad: bad argument");
   for (int j = 0; j < L; ++j) {
-    k_robin_grad_elem<<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
-        h->geo(), rho_node, T, L, j, h_coef, t_env, p, q, h->fe.as<double>());
+    TOPT_HEAT_NL(h, (k_robin_grad_elem<NL_><<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
+                        h->geo(), rho_node, T, L, j, h_coef, t_env, p, q, h->fe.as<double>())));
     TOPT_CHECK_LAUNCH("k_robin_grad_elem");
     k_node_gather<<<h->grid(h->n_nodes), kHB, 0, h->stream>>>(
-        h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem,
+        h->n_nodes, h->node_ptr.as<int32_t>(), h->adj.as<int32_t>(), h->n_elem, h->nloc,
         h->fe.as<double>(), 1.0, h->nodal.as<double>());
     TOPT_CHECK_LAUNCH("k_node_gather");
-    k_nodal_to_elem<<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
-        h->geo(), h->node_ptr.as<int32_t>(), h->nodal.as<double>(), L, j, grad);
+    TOPT_HEAT_NL(h, (k_nodal_to_elem<NL_><<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
+                        h->geo(), h->node_ptr.as<int32_t>(), h->nodal.as<double>(), L, j,
+                        grad)));
     TOPT_CHECK_LAUNCH("k_nodal_to_elem");
   }
   return TOPT_OK;
@@ -587,7 +705,8 @@ int topt_heat_grad_dot(topt_heat* h, const double* X, const double* Y, int32_t L
   using namespace topt;
   if (!h || !X || !Y || !out || L < 1 || L > 64)
     return fail(TOPT_BAD_INPUT, "heat_grad_dot: bad argument");
-  k_grad_dot<<<h->grid(h->n_elem), kHB, 0, h->stream>>>(h->geo(), X, Y, L, out);
+  TOPT_HEAT_NL(h, (k_grad_dot<NL_><<<h->grid(h->n_elem), kHB, 0, h->stream>>>(
+                      h->geo(), X, Y, L, out)));
   TOPT_CHECK_LAUNCH("k_grad_dot");
   return TOPT_OK;
 }

@@ -140,6 +140,7 @@ SIGNATURES = {
     "topt_reduce_dot": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
     "topt_reduce_dot_noalloc": (C.c_int, [_I64, _P, _P, C.POINTER(_D), _P]),
     "topt_heat_create": (C.c_int, [_I64, _I64, _P, _P, _I32, C.POINTER(_P)]),
+    "topt_heat_create_mesh": (C.c_int, [_I64, _I64, _I32, _P, _P, _I32, C.POINTER(_P)]),
     "topt_heat_destroy": (None, [_P]),
     "topt_heat_set_stream": (C.c_int, [_P, _P]),
     "topt_heat_set_surface": (C.c_int, [_P, _I64, _P, _P]),

@@ -28,11 +28,14 @@ Drop-in for ``FEM_SimpLinearHeatConduction`` (sktopt/fea/solver_heat.py:
   interpolation) plus, for the compliance objective with Robin data, the
   explicit Robin term.
 
-The volume integrals of the Robin and heat-exchange forms use the 2x2x2
-Gauss rule of the element matrices; Robin data needs axis-aligned hexahedra.
-The nodal density average follows the reference's pairing of ``t.ravel()``
-with ``np.repeat(rho, 8)`` (node t[a, e] receives rho[(a n_elem + e) // 8]);
-``nodal_pairing="element"`` gives node t[a, e] the density of element e.
+The volume integrals of the Robin and heat-exchange forms use the
+quadrature of a basis with intorder 2: the 2x2x2 Gauss rule on hexahedra
+(axis-aligned), the 4-point degree-2 rule on P1 tetrahedra.  Robin facets
+are rows (element, axis, side) on hexahedra and (element, local face) on
+tetrahedra.  The nodal density average follows the reference's pairing of
+``t.ravel()`` with ``np.repeat(rho, nloc)`` (node t[a, e] receives
+rho[(a n_elem + e) // nloc]); ``nodal_pairing="element"`` gives node t[a, e]
+the density of element e.
 """
 from __future__ import annotations
 
@@ -44,7 +47,7 @@ import torch
 
 from .. import _native as N
 from .._device import as_device, default_device, stream_handle, write_back
-from ..mesh.grid import HEX_OFFSETS, hex_face_local_nodes
+from ..mesh.grid import HEX_OFFSETS, TET_FACES, hex_face_local_nodes
 from . import composer
 from .engine import FemEngine, SolveStats
 from .solver_elastic import LinearSolverConfig, normalize_linear_solver_config
@@ -56,10 +59,26 @@ def _p(t):
     return C.c_void_p(t.data_ptr())
 
 
+def _tri_area(mesh, e, loc):
+    X = mesh.p[:, mesh.t[loc, e]]
+    return 0.5 * float(np.linalg.norm(np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0])))
+
+
 def surface_robin_matrices(mesh, faces, h):
-    """Per-face h * int N_a N_b over one hexahedron face (task_heat.py:
-    106-134), in the owning element's local numbering: the tensor product of
-    the two edge mass matrices L/6 [[2, 1], [1, 2]].  Returns (n_faces, 64)."""
+    """Per-face h * int N_a N_b over one element face (task_heat.py:
+    106-134), in the owning element's local numbering.  Hexahedron faces
+    (rows (element, axis, side)): the tensor product of the two edge mass
+    matrices L/6 [[2, 1], [1, 2]]; tetrahedron faces (rows (element, local
+    face)): A/12 (1 + delta_ab).  Returns (n_faces, nloc^2)."""
+    if mesh.kind != "hex":
+        out = np.zeros((len(faces), 4, 4))
+        for k, (e, f) in enumerate(faces):
+            loc = TET_FACES[int(f)]
+            a = _tri_area(mesh, int(e), loc)
+            for i, ni in enumerate(loc):
+                for j, nj in enumerate(loc):
+                    out[k, ni, nj] = h * a / 12.0 * (2.0 if i == j else 1.0)
+        return out.reshape(len(faces), 16)
     out = np.zeros((len(faces), 8, 8))
     for k, (e, axis, side) in enumerate(faces):
         loc = hex_face_local_nodes(int(axis), int(side))
@@ -76,8 +95,14 @@ def surface_robin_matrices(mesh, faces, h):
 
 def surface_robin_load(mesh, faces, h, t_env):
     """h T_env int N_a over the faces (task_heat.py:121-135): a quarter of
-    the face area at each of its nodes."""
+    the face area at each node of a hexahedron face, a third at each node of
+    a triangle."""
     f = np.zeros(mesh.nnodes)
+    if mesh.kind != "hex":
+        for e, fc in faces:
+            loc = TET_FACES[int(fc)]
+            np.add.at(f, mesh.t[loc, int(e)], h * t_env * _tri_area(mesh, int(e), loc) / 3.0)
+        return f
     for e, axis, side in faces:
         loc = hex_face_local_nodes(int(axis), int(side))
         ax = [d for d in range(3) if d != axis]
@@ -90,8 +115,6 @@ class HeatRobinOps:
     """The ``topt_heat`` handle: Robin element matrices and heat objectives."""
 
     def __init__(self, mesh, pairing: str = "reference", device=None):
-        if mesh.kind != "hex":
-            raise NotImplementedError("Robin terms and heat-exchange objectives need hexahedra")
         self.lib = N.load()
         self.device = device or default_device()
         self.mesh = mesh
@@ -99,10 +122,11 @@ class HeatRobinOps:
         p = np.ascontiguousarray(mesh.p, dtype=np.float64)
         h = C.c_void_p()
         with torch.cuda.device(self.device):
-            N.check(self.lib.topt_heat_create(mesh.nnodes, mesh.nelements,
-                                              t.ctypes.data_as(C.c_void_p),
-                                              p.ctypes.data_as(C.c_void_p),
-                                              0 if pairing == "reference" else 1, C.byref(h)))
+            N.check(self.lib.topt_heat_create_mesh(mesh.nnodes, mesh.nelements, t.shape[0],
+                                                   t.ctypes.data_as(C.c_void_p),
+                                                   p.ctypes.data_as(C.c_void_p),
+                                                   0 if pairing == "reference" else 1,
+                                                   C.byref(h)))
         self.h = h
 
     def close(self):

@@ -245,7 +245,8 @@ class LinearHeatConduction(FEMDomain):
     value on the same Dirichlet nodes).  ``emit``: optional volumetric
     source (nodal load; the reference has none).  Robin data
     (task_common.py:76-81): ``robin_faces`` -- an (n, 3) array of hexahedron
-    faces (element, axis, side) or a list of such groups -- with
+    faces (element, axis, side), on tetrahedra an (n, 2) array of faces
+    (element, local face), or a list of such groups -- with
     ``robin_coefficient`` h and ``robin_bc_value`` T_env (scalars, or one per
     group for the surface terms).  ``objective``: "compliance",
     "heat_exchange" or "averaged_temp"."""
@@ -278,7 +279,8 @@ class LinearHeatConduction(FEMDomain):
         if self.robin_faces is None:
             return []
         g = self.robin_faces if isinstance(self.robin_faces, list) else [self.robin_faces]
-        return [np.asarray(x, dtype=np.int64).reshape(-1, 3) for x in g]
+        w = 3 if self.mesh.kind == "hex" else 2
+        return [np.asarray(x, dtype=np.int64).reshape(-1, w) for x in g]
 
     @classmethod
     def from_nodes(cls, mesh, dirichlet_nodes, emit, design_elements, k=1.0,
@@ -294,7 +296,8 @@ class LinearHeatConduction(FEMDomain):
         rob_el = None
         if robin_faces is not None:
             groups = robin_faces if isinstance(robin_faces, list) else [robin_faces]
-            allf = np.concatenate([np.asarray(g, dtype=np.int64).reshape(-1, 3)
+            w = 3 if mesh.kind == "hex" else 2
+            allf = np.concatenate([np.asarray(g, dtype=np.int64).reshape(-1, w)
                                    for g in groups])
             rob_el = np.unique(allf[:, 0])
             if design_robin_boundary is False:
@@ -313,16 +316,15 @@ class LinearHeatConduction(FEMDomain):
     def from_facets(cls, mesh, dirichlet_facets, dirichlet_values, robin_facets,
                     robin_coefficient, robin_bc_value, design_robin_boundary, design_elements,
                     k, objective="compliance", avg_temp_weight=0.0, emit=None):
-        """task_heat.py:172-250 with facets as rows (element, local face);
-        Robin facets must be hexahedron faces."""
+        """task_heat.py:172-250 with facets as rows (element, local face)."""
         from .grid import facet_nodes_of, facets_to_faces
         groups = _group_list(dirichlet_facets)
         dn = np.unique(np.concatenate([facet_nodes_of(mesh, f).ravel() for f in groups]))
         rob = None
         if robin_facets is not None:
-            if mesh.kind != "hex":
-                raise NotImplementedError("Robin facets need a hexahedral mesh")
-            rob = [facets_to_faces(f) for f in _group_list(robin_facets)]
+            rob = [facets_to_faces(f) if mesh.kind == "hex" else
+                   np.asarray(f, dtype=np.int64).reshape(-1, 2)
+                   for f in _group_list(robin_facets)]
         return cls.from_nodes(mesh, dn, emit, design_elements, k=k,
                               dirichlet_values=dirichlet_values, robin_faces=rob,
                               robin_coefficient=robin_coefficient,
@@ -351,11 +353,17 @@ class LinearHeatConduction(FEMDomain):
         ``dirichlet`` / ``robin`` are point predicates (get_points_in_range)
         or lists of them, applied to boundary-facet midpoints."""
         dl = dirichlet if isinstance(dirichlet, list) else [dirichlet]
-        dn = np.unique(np.concatenate([face_nodes(mesh, boundary_faces(mesh, f)) for f in dl]))
+        if mesh.kind == "hex":
+            faces_of, nodes_of = boundary_faces, face_nodes
+        else:   # tetrahedra: facets as rows (element, local face)
+            from .grid import boundary_facets, facet_nodes_of
+            faces_of, nodes_of = boundary_facets, facet_nodes_of
+        dn = np.unique(np.concatenate([np.ravel(nodes_of(mesh, faces_of(mesh, f)))
+                                       for f in dl]))
         rob = None
         if robin is not None:
             rl = robin if isinstance(robin, list) else [robin]
-            rob = [boundary_faces(mesh, f) for f in rl]
+            rob = [faces_of(mesh, f) for f in rl]
         if design_elements is None:
             design_elements = np.arange(mesh.nelements)
         return cls.from_nodes(mesh, dn, emit, design_elements, k=k,

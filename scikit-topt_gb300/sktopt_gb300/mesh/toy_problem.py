@@ -70,6 +70,23 @@ def heat_plate(nx=40, ny=40, nz=5, objective="compliance", avg_temp_weight=0.0,
         objective=objective, avg_temp_weight=avg_temp_weight)
 
 
+def heat_plate_tet(nx=40, ny=40, nz=5, objective="compliance", avg_temp_weight=0.0,
+                   dirichlet_values=600.0, robin=True, jitter=0.2, seed=0):
+    """The heat plate of ``heat_plate`` meshed with P1 tetrahedra: the
+    nx x ny x nz grid split into 6 tetrahedra per cell, interior nodes
+    jittered by U(-jitter h, jitter h) (seeded), Robin on the x = 0 and y = 8
+    boundary facets, T = 600 on the boundary facets near the corner."""
+    from .grid import get_points_in_range as rng
+    lx, ly, lz = 8.0, 8.0, 1.0
+    mesh = create_box_tet(nx, ny, nz, lx, ly, lz, jitter=jitter, seed=seed)
+    return LinearHeatConduction.from_boundaries(
+        mesh, rng((lx - lx / 20, lx), (0.0, ly / 20), (0.0, lz)), dirichlet_values,
+        [rng((0.0, 0.0), (0.0, ly), (0.0, lz)), rng((0.0, lx), (ly, ly), (0.0, lz))]
+        if robin else None,
+        4.0e-5 if robin else None, 300.0 if robin else None, True, 10.0,
+        objective=objective, avg_temp_weight=avg_temp_weight)
+
+
 def multi_load_tet(nx=160, ny=80, nz=40, lx=2.0, ly=1.0, lz=1.0, jitter=0.2, seed=0,
                    E=1.0, nu=0.3):
     """Box meshed with jittered P1 tets, bottom face clamped, 4 point-load cases."""

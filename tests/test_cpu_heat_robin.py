@@ -213,6 +213,69 @@ def test_heat_plugin_argument_checks():
     m = create_box_tet(3, 2, 2, 1.0, 1.0, 1.0)
     from sktopt_gb300.mesh import boundary_facets
     f = boundary_facets(m)[:2]
-    with pytest.raises(NotImplementedError):
-        LinearHeatConduction.from_facets(m, f, 1.0, f, 1e-3, 300.0, True,
-                                         np.arange(m.nelements), 1.0)
+    # tetrahedra: Robin facets stay rows (element, local face)
+    tt = LinearHeatConduction.from_facets(m, f, 1.0, f, 1e-3, 300.0, True,
+                                          np.arange(m.nelements), 1.0)
+    assert [g.shape for g in tt.robin_groups] == [(2, 2)]
+    np.testing.assert_array_equal(tt.robin_groups[0], f)
+
+
+# --- P1 tetrahedra --------------------------------------------------------------
+def _tet_plate(n=(6, 6, 2)):
+    from oracle import mesh as omesh
+    from sktopt_gb300.mesh import toy_problem
+    t = toy_problem.heat_plate_tet(*n)
+    m = omesh.GridMesh(t.mesh.p, t.mesh.t, "tet", None, None, None)
+    return t, m
+
+
+def test_tet_quadrature_linear_field_exact():
+    t, m = _tet_plate()
+    Q = hr.tet_quadrature(m)
+    assert abs(Q[2].sum() - 64.0) <= 1e-12 * 64.0           # the plate's volume
+    a = np.array([0.3, -0.2, 0.5])
+    rho_n = 0.1 + a @ m.p * 0.01
+    den = hr.hx_den(m, Q, rho_n)
+    assert abs(den - 0.01 * np.linalg.norm(a) * 64.0) <= 1e-12 * den
+    # the rule integrates quadratics exactly: int N_a N_b = V / 20 (1 + delta)
+    N, dN, wd = Q
+    M = np.einsum("eq,qa,qb->eab", wd, N, N)
+    V = wd.sum(axis=1)
+    want = V[:, None, None] / 20.0 * (np.ones((4, 4)) + np.eye(4))
+    np.testing.assert_allclose(M, want, rtol=1e-13)
+
+
+def test_tet_surface_robin_sums_and_product_match():
+    from sktopt_gb300.fea.solver_heat import surface_robin_load, surface_robin_matrices
+    t, m = _tet_plate((5, 4, 3))
+    for faces, area in zip(t.robin_groups, (8.0 * 1.0, 8.0 * 1.0)):
+        Me, load = hr.surface_robin(m, faces, 2.0, 300.0)
+        assert abs(Me.sum() - 2.0 * area) <= 1e-12 * area
+        assert abs(load.sum() - 2.0 * 300.0 * area) <= 1e-10 * area
+        np.testing.assert_allclose(surface_robin_matrices(t.mesh, faces, 2.0).reshape(-1, 4, 4),
+                                   Me, rtol=1e-13, atol=1e-20)
+        np.testing.assert_allclose(surface_robin_load(t.mesh, faces, 2.0, 300.0), load,
+                                   rtol=1e-13, atol=1e-18)
+
+
+def test_tet_explicit_robin_gradient_finite_differences():
+    t, m = _tet_plate((4, 4, 2))
+    Q = hr.tet_quadrature(m)
+    rng = np.random.default_rng(8)
+    rho_n = rng.uniform(0.2, 0.8, m.nnodes)
+    T = rng.uniform(250.0, 650.0, m.nnodes)
+    h, te, p, q = 4e-5, 300.0, 3.0, 4.0
+    N, dN, wd = Q
+
+    def G(r):
+        rq, g = hr._at_qp(N, dN, m, r)
+        tq, _ = hr._at_qp(N, dN, m, T)
+        iface = np.sqrt(np.sum(g ** 2, axis=2))
+        return float(np.sum(wd * h * rq ** p * (1 - rq) ** q * iface * (2 * te * tq - tq * tq)))
+
+    grad = hr.robin_explicit_grad(m, Q, rho_n, T, h, te, p, q)
+    for n in rng.choice(m.nnodes, 6, replace=False):
+        e = np.zeros(m.nnodes)
+        e[n] = 1e-6
+        fd = (G(rho_n + e) - G(rho_n - e)) / 2e-6
+        assert abs(fd - grad[n]) <= 1e-6 * max(abs(grad).max(), 1e-300), (n, fd, grad[n])

@@ -166,3 +166,53 @@ def test_heat_robin_oc_loop_matches_oracle(native_lib, objective):
         assert abs(c - c_ref) <= 1e-8 * abs(c_ref), (k, c, c_ref)
         atol = 5e-6 if objective == "compliance" else 1e-7
         np.testing.assert_allclose(opt._state.rho.cpu().numpy(), ref.rho, rtol=0, atol=atol)
+
+
+def _tet_pair(n, objective, avg_w):
+    from oracle import mesh as omesh
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.heat_plate_tet(*n, objective=objective, avg_temp_weight=avg_w)
+    m = omesh.GridMesh(tsk.mesh.p, tsk.mesh.t, "tet", None, None, None)
+    pb = hr.HeatRobinProblem(m, np.unique(np.asarray(tsk.dirichlet_nodes)), 600.0, k0=10.0,
+                             robin_faces=[np.asarray(g) for g in tsk.robin_groups],
+                             robin_coefficient=4.0e-5, robin_bc_value=300.0,
+                             objective=objective, avg_temp_weight=avg_w)
+    return tsk, m, pb
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("objective,avg_w", [("compliance", 0.0), ("heat_exchange", 0.5),
+                                             ("averaged_temp", 0.0)])
+def test_heat_robin_tetrahedra_match_oracle(native_lib, objective, avg_w, precision):
+    """The plate meshed with jittered P1 tetrahedra: surface Robin terms on
+    triangles, virtual Robin and heat-exchange forms with the 4-point rule,
+    against the oracle's tetrahedral restatement (same tolerances as the
+    hexahedral plate)."""
+    import torch
+    from sktopt_gb300.fea.solver_heat import HeatRobinOps
+    tsk, m, pb = _tet_pair((10, 10, 2), objective, avg_w)
+    assert not tsk.mesh.has_grid or tsk.mesh.kind == "tet"
+    rho = np.random.default_rng(21).uniform(0.1, 1.0, m.nelements)
+    # nodal average: same summation order, bitwise
+    ops = HeatRobinOps(tsk.mesh, "reference", device=_dev())
+    out = torch.empty(m.nnodes, dtype=torch.float64, device=_dev())
+    ops.nodal_average(torch.from_numpy(rho).to(_dev()), out)
+    assert np.array_equal(out.cpu().numpy(), hr.nodal_average(m, rho, "reference")[0])
+    p, kmin = 3.0, 10.0 * 1e-3
+    J_ref, T_ref = pb.objectives(rho, p, kmin)
+    en_ref = pb.energy(rho, p, kmin, T_ref)
+    dc_ref = pb.custom_sensitivity(rho, p, kmin, T_ref)
+    fem = _fem(tsk, precision)
+    u = np.zeros((tsk.n_dof, 1))
+    J = fem.objectives_multi_load(rho, p, u)
+    K, _, _ = pb.operator(rho, p, kmin)
+    aT = np.abs(T_ref[:, 0])
+    floor = 4 * np.finfo(float).eps * (aT @ (abs(K) @ aT))
+    tol = (1e-9 if objective == "heat_exchange" else 1e-10) if precision == "fp64" else 1e-6
+    assert abs(J[0] - J_ref[0]) <= tol * abs(J_ref[0]) + floor, (J, J_ref, floor)
+    np.testing.assert_allclose(u, T_ref, rtol=0, atol=1e-8 * np.abs(T_ref).max())
+    vtol = 1e-8 if precision == "fp64" else 1e-5
+    if objective != "compliance":
+        assert _rel(fem.lam.cpu().numpy(), pb.lam) <= vtol
+    assert _rel(fem.energy_multi_load(rho, p, u), en_ref) <= vtol
+    assert _rel(fem.compliance_sensitivity_multi_load(rho, p, u), dc_ref) <= vtol
