@@ -136,6 +136,13 @@ int topt_fem_set_element_extra(topt_fem* h, const double* extra);
  * so the solve ends with TOPT_NONFINITE).  No reference counterpart: the
  * reference assembles with scikit-fem and multiplies with SciPy. */
 int topt_fem_set_mf_kernel(topt_fem* h, int32_t kind);
+/* V-cycle replay: on = 1 (the default) records one multigrid
+ * preconditioner application as a CUDA graph after the first application of
+ * each operator update and replays it (one graph launch per application
+ * instead of one launch per kernel); on = 0 launches every kernel.  Same
+ * kernels, same arguments, same results.  No reference counterpart (PyAMG's
+ * V-cycle is host code, solver_elastic.py:84-103). */
+int topt_fem_set_vcycle_graphs(topt_fem* h, int32_t on);
 int topt_fem_mf_error(topt_fem* h, int32_t* mf_error);
 
 /* Launch shapes, for an autotuner (no reference counterpart; none of them

@@ -511,10 +511,26 @@ struct ChebParams {
 };
 
 // Rebuild level values (level 0 from coef) and the hierarchy of precision T.
+// The recorded V-cycles hold the operator values, Chebyshev bounds and
+// launch shapes of the hierarchy they were recorded on.
+static void vcycle_graphs_stale(topt_fem* h) {
+  for (VcycleGraph& g : h->vcg) g.valid = false;
+  h->vc_direct[0] = h->vc_direct[1] = 0;
+}
+
+static void vcycle_graphs_free(topt_fem* h) {
+  for (VcycleGraph& g : h->vcg) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = VcycleGraph();
+  }
+  h->vc_direct[0] = h->vc_direct[1] = 0;
+}
+
 template <typename T>
 static int refresh(topt_fem* h, Hier<T>& H) {
   int rc;
   const int nlev = (int)h->ls.size();
+  vcycle_graphs_stale(h);
   if (!H.built) {
     H.lv.resize(nlev);
     for (int li = 0; li < nlev; ++li)
@@ -733,6 +749,71 @@ static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b
   return smooth_post<T>(h, li, H, L, degree, b, x);
 }
 
+// z = V-cycle(r).  The first application after a refresh runs directly
+// (it also sets the kernels' shared-memory attributes); the next one records
+// the V-cycle on the private stream, and later ones replay the graph on the
+// handle's stream: one launch instead of the 5 to 10 kernels per level.
+template <typename T>
+static int vcycle_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int degree) {
+  constexpr bool f32 = std::is_same<T, float>::value;
+  if (!h->vc_graphs || h->vc_direct[f32] == 0) {
+    ++h->vc_direct[f32];
+    return vcycle<T>(h, 0, H, L, degree, r, z, false);
+  }
+  VcycleGraph* g = nullptr;
+  for (VcycleGraph& c : h->vcg)
+    if (c.exec && c.fp32 == f32 && c.r == r && c.z == z && c.L == L && c.degree == degree &&
+        c.cheb_ratio == h->cheb_ratio) {
+      g = &c;
+      break;
+    }
+  if (!g) {   // a free slot, else the least recently used one
+    g = &h->vcg[0];
+    for (VcycleGraph& c : h->vcg) {
+      if (!c.exec) { g = &c; break; }
+      if (c.used < g->used) g = &c;
+    }
+    if (g->exec) cudaGraphExecDestroy(g->exec);
+    *g = VcycleGraph();
+    g->fp32 = f32; g->r = r; g->z = z; g->L = L; g->degree = degree;
+    g->cheb_ratio = h->cheb_ratio;
+  }
+  if (!g->valid) {
+    if (!h->cap) TOPT_CUDA(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+    TOPT_CUDA(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal));
+    cudaStream_t user = h->stream;
+    h->stream = h->cap;
+    const int rc = vcycle<T>(h, 0, H, L, degree, r, z, false);
+    h->stream = user;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(h->cap, &graph);
+    if (rc || ec != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      if (rc) return rc;
+      return fail_cuda((int)ec, "vcycle capture");
+    }
+    if (g->exec) {
+      cudaGraphExecUpdateResultInfo info;
+      if (cudaGraphExecUpdate(g->exec, graph, &info) != cudaSuccess) {
+        (void)cudaGetLastError();
+        cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+      }
+    }
+    cudaError_t ei = cudaSuccess;
+    if (!g->exec) ei = cudaGraphInstantiate(&g->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {
+      g->exec = nullptr;
+      return fail_cuda((int)ei, "vcycle graph instantiate");
+    }
+    g->valid = true;
+  }
+  g->used = ++h->vc_clock;
+  TOPT_CUDA(cudaGraphLaunch(g->exec, h->stream));
+  return TOPT_OK;
+}
+
 // ---------------------------------------------------------------- PCG
 // z = M^-1 r (V-cycle or block Jacobi); r.z into reducer slot `slot` unless
 // slot < 0.
@@ -743,7 +824,7 @@ static int precond_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int p
   LevelNum<T>& N0 = H.lv[0];
   const int bs = h->bs;
   if (precond == 1 && h->ls.size() > 1) {
-    int rc2 = vcycle<T>(h, 0, H, L, degree, r, z, false);
+    int rc2 = vcycle_apply<T>(h, H, L, r, z, degree);
     if (rc2) return rc2;
     return slot < 0 ? TOPT_OK : dot<T>(h, h->n_dof, L, r, z, slot);
   }
@@ -1344,6 +1425,8 @@ void topt_fem_destroy(topt_fem* h) {
   if (h->ev_fork) cudaEventDestroy(h->ev_fork);
   if (h->ev_join) cudaEventDestroy(h->ev_join);
   if (h->aux) cudaStreamDestroy(h->aux);
+  vcycle_graphs_free(h);
+  if (h->cap) cudaStreamDestroy(h->cap);
   delete h;
 }
 
@@ -1366,6 +1449,14 @@ int topt_fem_set_mf_kernel(topt_fem* h, int32_t kind) {
   if (kind < 0 || kind > 1)
     return fail(TOPT_BAD_INPUT, "fem_set_mf_kernel: kind must be 0 (FMA) or 1 (tensor cores)");
   h->mf_kernel = kind;
+  vcycle_graphs_stale(h);
+  return TOPT_OK;
+}
+
+int topt_fem_set_vcycle_graphs(topt_fem* h, int32_t on) {
+  if (!h) return fail(TOPT_BAD_INPUT, "fem_set_vcycle_graphs: null handle");
+  h->vc_graphs = on != 0;
+  vcycle_graphs_free(h);
   return TOPT_OK;
 }
 
@@ -1472,6 +1563,7 @@ int topt_fem_set_mf_tile(topt_fem* h, int32_t ty) {
     return fail(TOPT_BAD_INPUT, "fem_set_mf_tile: ty must be 0 (automatic), 16, 27 or 32");
   if (!h->mf) return fail(TOPT_BAD_INPUT, "fem_set_mf_tile: no matrix-free operator");
   h->mf_ty = ty ? ty : mf_pick_ty(h->mfg.ny + 1);
+  vcycle_graphs_stale(h);
   return TOPT_OK;
 }
 
@@ -1482,6 +1574,7 @@ int topt_fem_set_row_mapping(topt_fem* h, int32_t level, int32_t mapping) {
   if (mapping < 0 || mapping > 3 || (mapping == 2 && h->bs != 3))
     return fail(TOPT_BAD_INPUT, "fem_set_row_mapping: mapping must be 0..3 (2 needs bs 3)");
   h->ls[level].row_map = mapping;
+  vcycle_graphs_stale(h);
   return TOPT_OK;
 }
 

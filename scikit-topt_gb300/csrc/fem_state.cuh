@@ -75,6 +75,22 @@ struct Hier {
   DevBuf dense_scratch;   // FP64 copy of the coarsest operator for its inverse
 };
 
+// One preconditioner application (a whole V-cycle) recorded as a CUDA graph
+// and replayed while the hierarchy, the operands and the smoother stay the
+// same; a hierarchy refresh marks it stale and the next application after the
+// first re-records it (cudaGraphExecUpdate when the kernel list is unchanged).
+struct VcycleGraph {
+  cudaGraphExec_t exec = nullptr;
+  const void* r = nullptr;
+  void* z = nullptr;
+  int L = 0, degree = 0;
+  bool fp32 = false;
+  double cheb_ratio = 0.0;
+  bool valid = false;
+  unsigned long long used = 0;   // last use (eviction order)
+};
+constexpr int kVcycleGraphs = 4;
+
 struct Reducer {
   DevBuf partials, counter, out;
   int max_blocks = 0;
@@ -146,6 +162,14 @@ struct topt_fem {
   topt::DevBuf mf_err;                 // set by k_mf_tc if an mbarrier wait times out
   topt::DevBuf nmask32;                // nmask widened to 32 bits (cp.async granule)
   topt::DevBuf nmask;                  // fixed flags of a node's 3 DOFs, bits 0-2
+  // V-cycles replayed as CUDA graphs (recorded on a private non-blocking
+  // stream, thread-local capture mode, so handles stepped from several host
+  // threads record concurrently)
+  bool vc_graphs = true;
+  cudaStream_t cap = nullptr;
+  topt::VcycleGraph vcg[topt::kVcycleGraphs];
+  unsigned long long vc_clock = 0;
+  int vc_direct[2] = {0, 0};           // direct applications since the last refresh (FP64, FP32)
 };
 
 namespace topt {

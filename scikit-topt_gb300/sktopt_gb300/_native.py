@@ -103,6 +103,7 @@ SIGNATURES = {
     "topt_fem_update": (C.c_int, [_P, _P, _D, _D, _D]),
     "topt_fem_set_interpolation": (C.c_int, [_P, _I32]),
     "topt_fem_set_mf_kernel": (C.c_int, [_P, _I32]),
+    "topt_fem_set_vcycle_graphs": (C.c_int, [_P, _I32]),
     "topt_fem_mf_error": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "topt_fem_set_element_extra": (C.c_int, [_P, _P]),
     "topt_fem_solve": (C.c_int, [_P, _P, _P, _I32, C.POINTER(SolveOpts),

@@ -11,9 +11,15 @@ design after another.  A design's work is ordered on its stream and every
 kernel is deterministic, so each design's trajectory is bit-identical to
 running it alone.
 
-The fine-level FP32 operator keeps its unit element matrix in the device's
-constant bank, shared by all handles: the designs of one batch must use
-elements of the same shape (the unit hexahedra of the cantilevers do).
+Every handle carries its own element matrices (the fine-level FP32
+operator takes its unit matrix as a kernel argument), so the designs of one
+batch may differ in element shape and material.
+
+The designs launch their V-cycles kernel by kernel: with 16 host threads
+stepping 256 designs the device is already kept busy by the other streams,
+and replaying the V-cycle as a CUDA graph (re-recorded after every operator
+update) measured slower, 352 against 403 design iterations per second
+(pass ``vcycle_graphs=True`` to use it anyway).
 """
 from __future__ import annotations
 
@@ -35,7 +41,7 @@ class BatchedDesigns:
     that stream.
     """
 
-    def __init__(self, makers, n_workers: int = 8, device=None):
+    def __init__(self, makers, n_workers: int = 8, device=None, vcycle_graphs: bool = False):
         self.device = device or default_device()
         self.n_workers = max(1, int(n_workers))
         self.streams = []
@@ -45,7 +51,8 @@ class BatchedDesigns:
             with torch.cuda.stream(s):
                 opt = make()
                 opt.parameterize()
-                opt.fem.engine   # build the FEM handle here, on the design's stream
+                # build the FEM handle here, on the design's stream
+                opt.fem.engine.set_vcycle_graphs(vcycle_graphs)
             self.streams.append(s)
             self.opts.append(opt)
         self._errors: list[BaseException] = []

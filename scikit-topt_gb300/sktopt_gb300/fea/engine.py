@@ -109,6 +109,11 @@ class FemEngine:
         (default), 1 tensor cores."""
         N.check(self.lib.topt_fem_set_mf_kernel(self.h, int(kind)))
 
+    def set_vcycle_graphs(self, on: bool):
+        """Replay the multigrid V-cycle as a CUDA graph (default on) or
+        launch its kernels one by one."""
+        N.check(self.lib.topt_fem_set_vcycle_graphs(self.h, 1 if on else 0))
+
     def mf_error(self) -> int:
         out = C.c_int32(0)
         N.check(self.lib.topt_fem_mf_error(self.h, C.byref(out)))
