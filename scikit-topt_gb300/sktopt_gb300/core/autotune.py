@@ -19,7 +19,8 @@ import threading
 import torch
 
 _CACHE: dict = {}
-_LOCK = threading.Lock()
+_LOCK = threading.Lock()        # guards _CACHE and _SHAPE_LOCKS
+_SHAPE_LOCKS: dict = {}         # one per problem shape: shapes tune concurrently
 
 
 def _key(engine) -> tuple:
@@ -98,9 +99,17 @@ def tune(engine, margin: float = 0.03, reps: int = 10) -> dict:
     key = _key(engine)
     with _LOCK:
         rec = _CACHE.get(key)
-        if rec is None:
-            rec = _measure(engine, margin, reps)
-            _CACHE[key] = rec
+        shape_lock = None if rec is not None else _SHAPE_LOCKS.setdefault(key, threading.Lock())
+    if rec is None:
+        # designs of other shapes (other host threads of a batch) tune
+        # meanwhile; a second design of this shape waits for the first
+        with shape_lock:
+            with _LOCK:
+                rec = _CACHE.get(key)
+            if rec is None:
+                rec = _measure(engine, margin, reps)
+                with _LOCK:
+                    _CACHE[key] = rec
     _apply(engine, rec)
     return rec
 
@@ -115,3 +124,4 @@ def cache() -> dict:
 def clear():
     with _LOCK:
         _CACHE.clear()
+        _SHAPE_LOCKS.clear()
