@@ -621,9 +621,9 @@ def probe_spmv(size):
 
 
 def probe_solve(size):
-    """Profiling target: one mixed state solve (default scheme) of the
-    cantilever of `size` at a seeded random density, after a warm-up solve,
-    inside the NVTX range "solve"."""
+    """Profiling target: one mixed state solve (default scheme, from a zero
+    guess) of the cantilever of `size` at a seeded random density, after a
+    warm-up solve of the same system, inside the NVTX range "solve"."""
     import numpy as np
     import torch
     from sktopt_gb300.fea.solver_elastic import FEM_SimpLinearElasticity, LinearSolverConfig
@@ -636,6 +636,7 @@ def probe_solve(size):
     rho = torch.from_numpy(0.01 + 0.99 * g.random(tsk.mesh.nelements)).to(dev)
     U = torch.zeros((3 * tsk.mesh.nnodes, 1), dtype=torch.float64, device=dev)
     fem.solve_device(rho, 3.0, U)
+    U.zero_()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("solve")
     c = fem.solve_device(rho, 3.0, U)

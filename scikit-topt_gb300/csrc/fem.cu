@@ -703,16 +703,16 @@ static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b
   if (!started) {
     const ChebParams cp(N.lmax, h->cheb_ratio);
     if (std::is_same<T, float>::value && h->mf && li == 0 && L == 1) {
-      // first step d = x = Dinv b / theta with the diagonal recomputed
+      // first step d = x = Dinv b / theta (the matrix-free level's kernel)
       ChebEp<float> ep;
       ep.kind = 3;
+      ep.dinv = (const float*)N.dinv.p;
       ep.c2 = (float)(1.0 / cp.theta);
       ep.dnew = (float*)N.d.p;
       ep.x = (float*)x;
-      k_cheb_mf<<<gridsize(h, Ls.n_nodes), kBlock, 0, h->stream>>>(
-          h->mfg, h->k0, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep,
-          (const float*)b);
-      TOPT_CHECK_LAUNCH("k_cheb_mf");
+      k_cheb_stored<<<gridsize(h, Ls.n_nodes), kBlock, 0, h->stream>>>(Ls.n_nodes, ep,
+                                                                      (const float*)b);
+      TOPT_CHECK_LAUNCH("k_cheb_stored");
     } else {
       TOPT_BSL_DISPATCH(bs, L, (k_cheb<T, BS_, L_><<<gridsize(h, Ls.n_nodes), kBlock, 0,
                                                     h->stream>>>(

@@ -184,6 +184,10 @@ __global__ void k_block_diag_inv(SellT sp, const T* __restrict__ vals, T* __rest
   }
 }
 
+// Elements of a thread's grid-stride sequence handled per pass by the
+// streaming vector kernels (loads of the pass issued together).
+constexpr int kStreamUnroll = 4;
+
 // --------------------------------------------------------------------------
 // Chebyshev smoothing step fused into the operator that produced the
 // residual r (= the operator kernel's output y, held in registers):
@@ -201,10 +205,22 @@ struct ChebEp {
 };
 
 // The update of one block row given its inverted diagonal block Dv.  kind 3
-// (first step from a zero guess): dn = c2 Dinv r, x = dn.
+// (first step from a zero guess): dn = c2 Dinv r, x = dn.  The old
+// direction and x of the row are loaded before anything is stored: the
+// buffers are not restrict-qualified, so loads placed after a store would be
+// issued one memory round trip at a time.
 template <typename T, int BS, int L>
 __device__ __forceinline__ void cheb_update(const ChebEp<T>& ep, int64_t row, const T* r,
                                             const T* Dv) {
+  const int64_t base = row * BS * L;
+  T dold[BS * L], xo[BS * L];
+  if (ep.kind == 2) {
+#pragma unroll
+    for (int q = 0; q < BS * L; ++q) {
+      dold[q] = ep.dold[base + q];
+      xo[q] = ep.x[base + q];
+    }
+  }
 #pragma unroll
   for (int c = 0; c < BS; ++c)
 #pragma unroll
@@ -212,7 +228,8 @@ __device__ __forceinline__ void cheb_update(const ChebEp<T>& ep, int64_t row, co
       T s = T(0);
 #pragma unroll
       for (int d = 0; d < BS; ++d) s += Dv[c * BS + d] * r[d * L + j];
-      const int64_t idx = row * BS * L + c * L + j;
+      const int q = c * L + j;
+      const int64_t idx = base + q;
       if (ep.kind == 1) {
         ep.dnew[idx] = ep.c2 * s;
       } else if (ep.kind == 3) {
@@ -220,10 +237,9 @@ __device__ __forceinline__ void cheb_update(const ChebEp<T>& ep, int64_t row, co
         ep.dnew[idx] = dn;
         ep.x[idx] = dn;
       } else {
-        const T dold = ep.dold[idx];
-        const T dn = ep.c1 * dold + ep.c2 * s;
+        const T dn = ep.c1 * dold[q] + ep.c2 * s;
         ep.dnew[idx] = dn;
-        ep.x[idx] += ep.add_old ? dn + dold : dn;
+        ep.x[idx] = xo[q] + (ep.add_old ? dn + dold[q] : dn);
       }
     }
 }
@@ -664,22 +680,19 @@ static __global__ void k_mf_diag_inv(MfGrid g, const float* __restrict__ K0,
   }
 }
 
-// Chebyshev step of the matrix-free fine level as a separate pass: the
-// inverted diagonal block is recomputed per node from the cell coefficients
-// (the same FP32 arithmetic as k_mf_diag_inv, so the same bits) instead of
-// being read, which saves 36 B per node.  m32: fixed-DOF bits per node.
-static __global__ void k_cheb_mf(MfGrid g, const K0f k0, const float* __restrict__ coef,
-                          const uint32_t* __restrict__ m32, ChebEp<float> ep,
-                          const float* __restrict__ r) {
+// Chebyshev step of the matrix-free fine level as a separate pass (ChebEp
+// kinds 1-3 on r), with the inverted diagonal blocks read from the level's
+// stored copy (ep.dinv, written by k_mf_diag_inv at every refresh).
+// Recomputing them per node from the cell coefficients instead measured
+// issue-bound on GB300 (about 470 instructions per node, 58-75 % issue
+// activity, 20.7 / 27.1 us on 1.05M nodes); reading them costs 36 B per
+// node.  Same blocks, same update: the same bits either way.
+static __global__ void k_cheb_stored(int64_t n, ChebEp<float> ep, const float* __restrict__ r) {
   TOPT_KERNEL_COUNT();
-  const int ny1 = g.ny + 1, nx1 = g.nx + 1;
-  const int nn = nx1 * ny1 * (g.nz + 1);
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < nn; a += gridDim.x * blockDim.x) {
-    const int iy = a % ny1, ix = (a / ny1) % nx1, iz = a / (ny1 * nx1);
-    float rv[3] = {r[(int64_t)a * 3], r[(int64_t)a * 3 + 1], r[(int64_t)a * 3 + 2]};
-    float Dv[9];
-    mf_node_dinv(g, k0, coef, (int)m32[a], ix, iy, iz, Dv);
-    cheb_update<float, 3, 1>(ep, a, rv, Dv);
+  for (int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; a < n;
+       a += (int64_t)gridDim.x * blockDim.x) {
+    const float rv[3] = {r[a * 3], r[a * 3 + 1], r[a * 3 + 2]};
+    cheb_epilogue<float, 3, 1>(ep, a, rv);
   }
 }
 
@@ -961,15 +974,42 @@ __global__ void k_fcg_update32(int64_t n, const double* __restrict__ rz,
   float tacc[L];
 #pragma unroll
   for (int j = 0; j < L; ++j) tacc[j] = 0.0f;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t S = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  // kStreamUnroll elements of the thread's sequence per pass, all loads
+  // first (memory-level parallelism); the sums keep the sequence's order
+  for (; i + (kStreamUnroll - 1) * S < n; i += kStreamUnroll * S) {
+    double uv[kStreamUnroll][L];
+    float pv[kStreamUnroll][L], qv[kStreamUnroll][L], rv[kStreamUnroll][L];
+#pragma unroll
+    for (int u = 0; u < kStreamUnroll; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int64_t q_ = (i + u * S) * L + j;
+        uv[u][j] = U[q_];
+        pv[u][j] = p[q_];
+        qv[u][j] = q[q_];
+        rv[u][j] = r[q_];
+      }
+#pragma unroll
+    for (int u = 0; u < kStreamUnroll; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int64_t q_ = (i + u * S) * L + j;
+        U[q_] = uv[u][j] + alpha[j] * (double)pv[u][j];
+        const float rn = rv[u][j] - alpha32[j] * qv[u][j];
+        r[q_] = rn;
+        tacc[j] += rn * rn;
+      }
+  }
+  for (; i < n; i += S) {
 #pragma unroll
     for (int j = 0; j < L; ++j) {
       const int64_t q_ = i * L + j;
       U[q_] += alpha[j] * (double)p[q_];
-      const float rv = r[q_] - alpha32[j] * q[q_];
-      r[q_] = rv;
-      tacc[j] += rv * rv;
+      const float rv1 = r[q_] - alpha32[j] * q[q_];
+      r[q_] = rv1;
+      tacc[j] += rv1 * rv1;
     }
   }
   double acc[L];
@@ -1019,8 +1059,28 @@ __global__ void k_fcg_direction(int64_t n, const double* __restrict__ qz,
 #pragma unroll
   for (int j = 0; j < L; ++j)
     beta[j] = (active[j] && pq[j] > 0.0) ? (T)(-qz[j] / pq[j]) : T(0);
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int64_t S = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (; i + (kStreamUnroll - 1) * S < n; i += kStreamUnroll * S) {
+    T zv[kStreamUnroll][L], pv[kStreamUnroll][L];
+#pragma unroll
+    for (int u = 0; u < kStreamUnroll; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        zv[u][j] = (T)z[(i + u * S) * L + j];
+        pv[u][j] = p[(i + u * S) * L + j];
+      }
+#pragma unroll
+    for (int u = 0; u < kStreamUnroll; ++u)
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        const int64_t q_ = (i + u * S) * L + j;
+        const T v = zv[u][j] + beta[j] * pv[u][j];
+        p[q_] = v;
+        if (p32) p32[q_] = (float)v;
+      }
+  }
+  for (; i < n; i += S) {
 #pragma unroll
     for (int j = 0; j < L; ++j) {
       const T v = (T)z[i * L + j] + beta[j] * p[i * L + j];

@@ -48,9 +48,8 @@ static int launch_mf(topt_fem* h, const float* x, const float* b, float* y, int 
                       : launch_mf_ty<MODE, DOT, true>(h, x, b, y, slot);
     if (rc) return rc;
     if (ep.kind) {
-      k_cheb_mf<<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(
-          h->mfg, h->k0, h->coef32.as<float>(), h->nmask32.as<uint32_t>(), ep, y);
-      TOPT_CHECK_LAUNCH("k_cheb_mf");
+      k_cheb_stored<<<gridsize(h, h->n_nodes), kBlock, 0, h->stream>>>(h->n_nodes, ep, y);
+      TOPT_CHECK_LAUNCH("k_cheb_stored");
     }
     return TOPT_OK;
   }
