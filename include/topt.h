@@ -164,6 +164,12 @@ int topt_fem_get_tuning(const topt_fem* h, int32_t* mf_tile, int32_t* mappings,
                         int32_t n_levels);
 int topt_fem_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x,
                         void* y);
+/* Average device time in microseconds of one topt_fem_spmv_level product
+ * (same arguments), measured over `reps` (1..1000) back-to-back products
+ * replayed as a CUDA graph, without host launch overhead: the launch-shape
+ * autotuner's measurement.  Synchronises the handle's stream. */
+int topt_fem_time_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x,
+                             void* y, int32_t reps, double* us);
 /* Nodes (block rows) of each of the first n_levels levels and whether the
  * level is the dense coarsest one. */
 int topt_fem_level_sizes(const topt_fem* h, int64_t* n_nodes, int32_t* dense,

@@ -1615,6 +1615,53 @@ int topt_fem_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x
                               "(FP32 for mixed handles, FP64 otherwise)");
 }
 
+// Device time of one level product, for the launch-shape autotuner: `reps`
+// back-to-back products recorded as a CUDA graph on the private stream and
+// timed with events around one replay (after a warm-up replay), so that host
+// launch overhead, which exceeds the kernel time on small levels, does not
+// enter the figure.
+int topt_fem_time_spmv_level(topt_fem* h, int32_t level, int32_t dtype, const void* x, void* y,
+                             int32_t reps, double* us) {
+  if (!h || !x || !y || !us) return fail(TOPT_BAD_INPUT, "fem_time_spmv_level: null argument");
+  if (reps < 1 || reps > 1000)
+    return fail(TOPT_BAD_INPUT, "fem_time_spmv_level: reps must be in 1..1000");
+  int rc = topt_fem_spmv_level(h, level, dtype, x, y);   // checks; sets kernel attributes
+  if (rc) return rc;
+  TOPT_CUDA(cudaStreamSynchronize(h->stream));
+  if (!h->cap) TOPT_CUDA(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
+  TOPT_CUDA(cudaStreamBeginCapture(h->cap, cudaStreamCaptureModeThreadLocal));
+  cudaStream_t user = h->stream;
+  h->stream = h->cap;
+  for (int r = 0; r < reps && !rc; ++r) rc = topt_fem_spmv_level(h, level, dtype, x, y);
+  h->stream = user;
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(h->cap, &graph);
+  if (rc || ec != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc ? rc : fail_cuda((int)ec, "fem_time_spmv_level capture");
+  }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return fail_cuda((int)ei, "fem_time_spmv_level instantiate");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, h->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e0, h->stream);
+  if (e == cudaSuccess) e = cudaGraphLaunch(exec, h->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(e1, h->stream);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  float ms = 0.0f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaGraphExecDestroy(exec);
+  if (e != cudaSuccess) return fail_cuda((int)e, "fem_time_spmv_level");
+  *us = 1e3 * (double)ms / reps;
+  return TOPT_OK;
+}
+
 int topt_fem_export_values(topt_fem* h, double* vals) {
   if (!h || !vals) return fail(TOPT_BAD_INPUT, "fem_export_values: null argument");
   if (!h->assembled) return fail(TOPT_BAD_INPUT, "fem_export_values: not assembled");

@@ -96,6 +96,7 @@ SIGNATURES = {
     "topt_fem_set_row_mapping": (C.c_int, [_P, _I32, _I32]),
     "topt_fem_get_tuning": (C.c_int, [_P, C.POINTER(_I32), _P, _I32]),
     "topt_fem_spmv_level": (C.c_int, [_P, _I32, _I32, _P, _P]),
+    "topt_fem_time_spmv_level": (C.c_int, [_P, _I32, _I32, _P, _P, _I32, _P]),
     "topt_fem_level_sizes": (C.c_int, [_P, _P, _P, _I32]),
     "topt_fem_destroy": (None, [_P]),
     "topt_fem_set_stream": (C.c_int, [_P, _P]),

@@ -4,9 +4,11 @@ Two launch shapes of the engine are free: the node rows per tile of the
 FP32-FMA fine-level operator (16, 27 or 32) and the threads per block row of
 each level's SELL products (a warp, three threads, or one thread).  The
 engine's rules pick them from the grid's y extent and the level size; this
-tuner times every candidate with CUDA events on the current stream (the
-engine's) and keeps the fastest when it beats the rule's choice by more than
-`margin`, once per problem shape.  The choices are cached process-wide, so
+tuner times every candidate on the device (``FemEngine.time_spmv_level``:
+back-to-back products replayed as a CUDA graph, so host launch overhead --
+larger than the kernel on the small levels -- does not decide) and keeps the
+fastest when it beats the rule's choice by more than `margin`, once per
+problem shape.  The choices are cached process-wide, so
 every design of a batch with the same shape, and a solo run of that shape,
 use the same launch shapes and compute the same bits.
 
@@ -30,17 +32,9 @@ def _key(engine) -> tuple:
     return (engine.bs, bool(engine.mixed), shape, engine.n_levels)
 
 
-def _time_us(fn, reps: int) -> float:
-    s = torch.cuda.current_stream()
-    for _ in range(2):
-        fn()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(s)
-    for _ in range(reps):
-        fn()
-    e1.record(s)
-    e1.synchronize()
-    return e0.elapsed_time(e1) * 1e3 / reps
+def _time_us(engine, li, x, y, reps: int) -> float:
+    # the better of two graph replays
+    return min(engine.time_spmv_level(li, x, y, reps) for _ in range(2))
 
 
 def _measure(engine, margin: float, reps: int) -> dict:
@@ -56,12 +50,12 @@ def _measure(engine, margin: float, reps: int) -> dict:
         g = torch.Generator(device=engine.device).manual_seed(li)
         x = torch.rand(n, dtype=dt, device=engine.device, generator=g)
         y = torch.empty_like(x)
-        run = lambda: engine.spmv_level(li, x, y)  # noqa: E731
+        run = lambda: _time_us(engine, li, x, y, reps)  # noqa: E731
         if li == 0 and rule["mf_tile"]:
             times = {}
             for ty in (16, 27, 32):
                 engine.set_mf_tile(ty)
-                times[ty] = _time_us(run, reps)
+                times[ty] = run()
             best = min(times, key=times.get)
             pick = best if times[best] < (1.0 - margin) * times[rule["mf_tile"]] \
                 else rule["mf_tile"]
@@ -73,7 +67,7 @@ def _measure(engine, margin: float, reps: int) -> dict:
         times = {}
         for m in cands:
             engine.set_row_mapping(li, m)
-            times[m] = _time_us(run, reps)
+            times[m] = run()
         best = min(times, key=times.get)
         auto = rule["row_mapping"][li]
         pick = best if times[best] < (1.0 - margin) * times[auto] else auto
@@ -91,7 +85,7 @@ def _apply(engine, rec: dict):
             engine.set_row_mapping(li, m)
 
 
-def tune(engine, margin: float = 0.03, reps: int = 10) -> dict:
+def tune(engine, margin: float = 0.03, reps: int = 20) -> dict:
     """Set the engine's launch shapes: measured once per problem shape (the
     engine must hold an operator, i.e. after an update), then reused from
     the process-wide cache.  Returns the record (choices, the rule's

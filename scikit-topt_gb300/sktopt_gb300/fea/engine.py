@@ -151,6 +151,19 @@ class FemEngine:
         N.check(self.lib.topt_fem_spmv_level(self.h, int(level), dt, C.c_void_p(x.data_ptr()),
                                              C.c_void_p(y.data_ptr())))
 
+    def time_spmv_level(self, level: int, x: torch.Tensor, y: torch.Tensor,
+                        reps: int = 20) -> float:
+        """Device time in microseconds of one ``spmv_level`` product, from
+        ``reps`` products replayed as a CUDA graph (no host launch overhead)."""
+        self._bind()
+        dt = N.TOPT_F32 if self.mixed else N.TOPT_F64
+        us = C.c_double(0.0)
+        N.check(self.lib.topt_fem_time_spmv_level(self.h, int(level), dt,
+                                                  C.c_void_p(x.data_ptr()),
+                                                  C.c_void_p(y.data_ptr()), int(reps),
+                                                  C.byref(us)))
+        return us.value
+
     def level_sizes(self) -> list:
         """Block rows (nodes) of every level of the hierarchy, and whether the
         level is the dense coarsest one (as (nodes, dense) pairs)."""

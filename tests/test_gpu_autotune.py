@@ -57,6 +57,27 @@ def test_launch_shapes_compute_the_same_operator(native_lib, mixed):
     assert eng.tuning() == rule
 
 
+def test_graph_timing_of_a_level_product(native_lib):
+    """The tuner's measurement: graph-replayed products leave y equal to one
+    direct product and give a positive time that orders a small level below
+    the fine level."""
+    eng = _engine((60, 20, 14))
+    sizes = eng.level_sizes()
+    times = []
+    for li, (nodes, dense) in enumerate(sizes):
+        if dense:
+            continue
+        x = torch.rand(nodes * 3, dtype=torch.float32, device=_dev())
+        ref = torch.empty_like(x)
+        eng.spmv_level(li, x, ref)
+        y = torch.zeros_like(x)
+        us = eng.time_spmv_level(li, x, y, reps=5)
+        assert np.isfinite(us) and us > 0.0
+        assert torch.equal(y, ref)
+        times.append(us)
+    assert times[-1] < times[0]
+
+
 def test_tuner_picks_once_per_shape(native_lib):
     from sktopt_gb300.core import autotune
     autotune.clear()
