@@ -1,7 +1,7 @@
 // The matrix-free FP32 fine-level operator of uniform hex grids: FP32-FMA
 // node tiles (k_mf_tile, the default) or the tcgen05 kernel of mf_tc.cu,
-// with the Chebyshev step fused into the operator that produces its
-// residual.
+// followed, when the caller asks for a Chebyshev step on the residual it
+// produced, by the separate pass k_cheb_stored.
 #include "fem_state.cuh"
 
 #include <algorithm>
