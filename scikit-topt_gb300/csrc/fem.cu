@@ -514,8 +514,10 @@ struct ChebParams {
 // The recorded V-cycles hold the operator values, Chebyshev bounds and
 // launch shapes of the hierarchy they were recorded on.
 static void vcycle_graphs_stale(topt_fem* h) {
-  for (VcycleGraph& g : h->vcg) g.valid = false;
-  h->vc_direct[0] = h->vc_direct[1] = 0;
+  for (VcycleGraph& g : h->vcg) {
+    g.valid = false;
+    g.direct_done = false;
+  }
 }
 
 static void vcycle_graphs_free(topt_fem* h) {
@@ -523,7 +525,6 @@ static void vcycle_graphs_free(topt_fem* h) {
     if (g.exec) cudaGraphExecDestroy(g.exec);
     g = VcycleGraph();
   }
-  h->vc_direct[0] = h->vc_direct[1] = 0;
 }
 
 template <typename T>
@@ -749,20 +750,20 @@ static int vcycle(topt_fem* h, int li, Hier<T>& H, int L, int degree, const T* b
   return smooth_post<T>(h, li, H, L, degree, b, x);
 }
 
-// z = V-cycle(r).  The first application after a refresh runs directly
-// (it also sets the kernels' shared-memory attributes); the next one records
-// the V-cycle on the private stream, and later ones replay the graph on the
-// handle's stream: one launch instead of the 5 to 10 kernels per level.
+// z = V-cycle(r).  After each refresh the first application for a given
+// (precision, r, z, load cases, degree, interval) runs directly (it also sets
+// the kernels' shared-memory attributes); the next one records the V-cycle
+// on the private stream, and later ones replay the graph on the handle's
+// stream: one launch instead of the 5 to 10 kernels per level.  Should a
+// recording or an instantiation be refused, the handle stops recording and
+// launches directly from then on (same kernels, same results).
 template <typename T>
 static int vcycle_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int degree) {
   constexpr bool f32 = std::is_same<T, float>::value;
-  if (!h->vc_graphs || h->vc_direct[f32] == 0) {
-    ++h->vc_direct[f32];
-    return vcycle<T>(h, 0, H, L, degree, r, z, false);
-  }
+  if (!h->vc_graphs) return vcycle<T>(h, 0, H, L, degree, r, z, false);
   VcycleGraph* g = nullptr;
   for (VcycleGraph& c : h->vcg)
-    if (c.exec && c.fp32 == f32 && c.r == r && c.z == z && c.L == L && c.degree == degree &&
+    if (c.r && c.fp32 == f32 && c.r == r && c.z == z && c.L == L && c.degree == degree &&
         c.cheb_ratio == h->cheb_ratio) {
       g = &c;
       break;
@@ -770,13 +771,18 @@ static int vcycle_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int de
   if (!g) {   // a free slot, else the least recently used one
     g = &h->vcg[0];
     for (VcycleGraph& c : h->vcg) {
-      if (!c.exec) { g = &c; break; }
+      if (!c.r) { g = &c; break; }
       if (c.used < g->used) g = &c;
     }
     if (g->exec) cudaGraphExecDestroy(g->exec);
     *g = VcycleGraph();
     g->fp32 = f32; g->r = r; g->z = z; g->L = L; g->degree = degree;
     g->cheb_ratio = h->cheb_ratio;
+  }
+  g->used = ++h->vc_clock;
+  if (!g->valid && !g->direct_done) {
+    g->direct_done = true;
+    return vcycle<T>(h, 0, H, L, degree, r, z, false);
   }
   if (!g->valid) {
     if (!h->cap) TOPT_CUDA(cudaStreamCreateWithFlags(&h->cap, cudaStreamNonBlocking));
@@ -787,12 +793,12 @@ static int vcycle_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int de
     h->stream = user;
     cudaGraph_t graph = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(h->cap, &graph);
-    if (rc || ec != cudaSuccess) {
+    if (rc) {
       if (graph) cudaGraphDestroy(graph);
-      if (rc) return rc;
-      return fail_cuda((int)ec, "vcycle capture");
+      return rc;
     }
-    if (g->exec) {
+    cudaError_t ei = ec;
+    if (ec == cudaSuccess && g->exec) {
       cudaGraphExecUpdateResultInfo info;
       if (cudaGraphExecUpdate(g->exec, graph, &info) != cudaSuccess) {
         (void)cudaGetLastError();
@@ -800,16 +806,17 @@ static int vcycle_apply(topt_fem* h, Hier<T>& H, int L, const T* r, T* z, int de
         g->exec = nullptr;
       }
     }
-    cudaError_t ei = cudaSuccess;
-    if (!g->exec) ei = cudaGraphInstantiate(&g->exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ei != cudaSuccess) {
+    if (ec == cudaSuccess && !g->exec) ei = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (ei != cudaSuccess) {   // recording refused: launch directly from now on
+      (void)cudaGetLastError();
       g->exec = nullptr;
-      return fail_cuda((int)ei, "vcycle graph instantiate");
+      vcycle_graphs_free(h);
+      h->vc_graphs = false;
+      return vcycle<T>(h, 0, H, L, degree, r, z, false);
     }
     g->valid = true;
   }
-  g->used = ++h->vc_clock;
   TOPT_CUDA(cudaGraphLaunch(g->exec, h->stream));
   return TOPT_OK;
 }

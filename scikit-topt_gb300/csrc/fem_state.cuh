@@ -77,8 +77,8 @@ struct Hier {
 
 // One preconditioner application (a whole V-cycle) recorded as a CUDA graph
 // and replayed while the hierarchy, the operands and the smoother stay the
-// same; a hierarchy refresh marks it stale and the next application after the
-// first re-records it (cudaGraphExecUpdate when the kernel list is unchanged).
+// same; a hierarchy refresh marks it stale, and the second application after
+// it re-records it (cudaGraphExecUpdate when the kernel list is unchanged).
 struct VcycleGraph {
   cudaGraphExec_t exec = nullptr;
   const void* r = nullptr;
@@ -86,7 +86,8 @@ struct VcycleGraph {
   int L = 0, degree = 0;
   bool fp32 = false;
   double cheb_ratio = 0.0;
-  bool valid = false;
+  bool direct_done = false;      // applied once directly since the last refresh
+  bool valid = false;            // exec holds the current hierarchy's V-cycle
   unsigned long long used = 0;   // last use (eviction order)
 };
 constexpr int kVcycleGraphs = 4;
@@ -169,7 +170,6 @@ struct topt_fem {
   cudaStream_t cap = nullptr;
   topt::VcycleGraph vcg[topt::kVcycleGraphs];
   unsigned long long vc_clock = 0;
-  int vc_direct[2] = {0, 0};           // direct applications since the last refresh (FP64, FP32)
 };
 
 namespace topt {
