@@ -19,7 +19,6 @@ import torch
 
 from ... import _native as N
 from ... import tools
-from ..._device import stream_handle
 from .common_density import DensityMethod, DensityMethod_OC_Config
 
 

@@ -3,7 +3,6 @@ time (the maximum over ranks) and the barrier returns on both."""
 import os
 import socket
 
-import pytest
 import torch.multiprocessing as mp
 
 
