@@ -382,9 +382,11 @@ int topt_node_to_elem(int64_t n_elem, int32_t nloc, const int32_t* t, const doub
  * Heat plugin on hexahedral and P1 tetrahedral meshes
  * (FEM_SimpLinearHeatConduction, sktopt/fea/solver_heat.py:306-625,
  * 705-980): Robin terms, heat-exchange objective and adjoint load, explicit
- * Robin gradient, grad T . grad lam.  Hexahedra must be axis-aligned boxes
- * (volume integrals with the 2x2x2 Gauss rule); tetrahedra take the 4-point
- * degree-2 rule.  Vectors are dev, n_nodes (x L row-major for several
+ * Robin gradient, grad T . grad lam.  Hexahedra take the 2x2x2 Gauss rule
+ * (axis-aligned boxes from their extents; any other hexahedron switches the
+ * handle to the trilinear map of the 8 nodes with the Jacobian at every
+ * Gauss point, which must be positive: TOPT_BAD_INPUT otherwise);
+ * tetrahedra take the 4-point degree-2 rule.  Vectors are dev, n_nodes (x L row-major for several
  * columns).
  * ---------------------------------------------------------------------- */
 typedef struct topt_heat topt_heat;

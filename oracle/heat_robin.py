@@ -301,10 +301,10 @@ class HeatRobinProblem:
         vals = dirichlet_values if isinstance(dirichlet_values, (list, tuple)) \
             else [dirichlet_values]
         self.values = [float(v) for v in vals]
-        if mesh.kind == "hex":
+        if mesh.kind == "hex" and fem._is_uniform_box(mesh):
             c = mesh.p[:, mesh.t[:, 0]]
             _, self.Kloc = fem.hex_element_matrices(c, 0.3)
-        else:
+        else:   # tetrahedra and general hexahedra: per-element matrices
             _, self.Kloc, _ = fem.element_matrices(mesh, 0.3)
         self.dofs = fem.element_dofs(mesh.t, 1)
         self.h = robin_coefficient

@@ -5,10 +5,12 @@
 // (sktopt/fea/solver_heat.py:306-625, 705-980).
 //
 // Every volume integral uses the quadrature of a basis with intorder 2: the
-// 2x2x2 Gauss rule on axis-aligned hexahedra (MeshHex local node order), the
-// 4-point degree-2 rule on tetrahedra (barycentric points (a, b, b, b),
-// a = (5 + 3 sqrt 5) / 20, b = (5 - sqrt 5) / 20, weights V / 4; the P1
-// gradients are constant per element and precomputed).  Nodal sums run over
+// 2x2x2 Gauss rule on hexahedra (MeshHex local node order; axis-aligned
+// boxes from their extents, other hexahedra from the trilinear map of their
+// 8 nodes, Jacobian per Gauss point), the 4-point degree-2 rule on
+// tetrahedra (barycentric points (a, b, b, b), a = (5 + 3 sqrt 5) / 20,
+// b = (5 - sqrt 5) / 20, weights V / 4; the P1 gradients are constant per
+// element and precomputed).  Nodal sums run over
 // a node -> (a, e) list kept in t.ravel() order (t is nloc x n_elem), so
 // they are deterministic, and the nodal density average adds in exactly the
 // order of the reference's np.add.at.
@@ -38,6 +40,7 @@ __host__ __device__ constexpr int hex_off(int a, int d) { return (0xF73850 >> (3
 template <int NL>
 struct QpT {
   double N[NL], gx[NL], gy[NL], gz[NL];
+  double w;   // quadrature weight times detJ
 };
 using Qp = QpT<8>;
 __device__ __forceinline__ void qpoint(int q, double G, double hx, double hy, double hz,
@@ -60,22 +63,76 @@ __device__ __forceinline__ void qpoint(int q, double G, double hx, double hy, do
   }
 }
 
+// The same at Gauss point q of a general hexahedron with nodes X (MeshHex
+// order): x(xi) = sum_a X_a N_a(xi) on the reference cube [0, 1]^3,
+// J = dx/dxi, physical gradients J^-T dN/dxi, weight detJ / 8.
+__device__ __forceinline__ void qpoint_general(int q, double G, const double (&X)[8][3],
+                                               Qp& o) {
+  const double x = (q >> 2) & 1 ? 0.5 + G : 0.5 - G;
+  const double y = (q >> 1) & 1 ? 0.5 + G : 0.5 - G;
+  const double z = q & 1 ? 0.5 + G : 0.5 - G;
+  double dr[8][3];
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    const double fx = hex_off(a, 0) ? x : 1.0 - x;
+    const double fy = hex_off(a, 1) ? y : 1.0 - y;
+    const double fz = hex_off(a, 2) ? z : 1.0 - z;
+    const double sx = hex_off(a, 0) ? 1.0 : -1.0;
+    const double sy = hex_off(a, 1) ? 1.0 : -1.0;
+    const double sz = hex_off(a, 2) ? 1.0 : -1.0;
+    o.N[a] = fx * fy * fz;
+    dr[a][0] = sx * fy * fz;
+    dr[a][1] = fx * sy * fz;
+    dr[a][2] = fx * fy * sz;
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) J[d][k] += X[a][d] * dr[a][k];
+  }
+  const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  const double id = 1.0 / det;
+  // Ji[k][d] = d xi_k / d x_d
+  const double Ji[3][3] = {
+      {c00 * id, (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id,
+       (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id},
+      {c01 * id, (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id,
+       (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id},
+      {c02 * id, (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id,
+       (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id}};
+#pragma unroll
+  for (int a = 0; a < 8; ++a) {
+    o.gx[a] = dr[a][0] * Ji[0][0] + dr[a][1] * Ji[1][0] + dr[a][2] * Ji[2][0];
+    o.gy[a] = dr[a][0] * Ji[0][1] + dr[a][1] * Ji[1][1] + dr[a][2] * Ji[2][1];
+    o.gz[a] = dr[a][0] * Ji[0][2] + dr[a][1] * Ji[1][2] + dr[a][2] * Ji[2][2];
+  }
+  o.w = 0.125 * det;
+}
+
 __device__ __forceinline__ double gauss_offset() { return 0.5 / sqrt(3.0); }
 
 struct Geo {
   const int32_t* t;     // nloc x ne
-  const double* hsz;    // hexahedra: 3 x ne extents
+  const double* hsz;    // axis-aligned hexahedra: 3 x ne extents
   const double* tg;     // tetrahedra: ne x 4 x 3 shape-function gradients
   const double* tv;     // tetrahedra: ne volumes
   int64_t ne;
+  const double* xyz;    // other hexahedra: node coordinates, 3 x nn (else null)
+  int64_t nn;
 };
 
-// Geometry of one element: hexahedron extents or tetrahedron gradients, and
-// the quadrature weight w (times detJ) shared by its points.
+// Geometry of one element: box extents, the 8 node coordinates of a general
+// hexahedron, or the tetrahedron gradients; and the quadrature weight w
+// (times detJ) of a box or tetrahedron, shared by its points.
 template <int NL>
 struct ElemG {
   double hx, hy, hz, w;
   double g[NL][3];
+  double X[8][3];
+  bool general;
 };
 
 template <int NL>
@@ -86,12 +143,22 @@ __device__ __forceinline__ void load_elem(const Geo& g, int64_t e, const double*
     node[a] = g.t[(int64_t)a * g.ne + e];
     v[a] = x ? x[node[a]] : 0.0;
   }
-  if (NL == 8) {
-    E.hx = g.hsz[e];
-    E.hy = g.hsz[g.ne + e];
-    E.hz = g.hsz[2 * g.ne + e];
-    E.w = 0.125 * (E.hx * E.hy * E.hz);
+  if constexpr (NL == 8) {
+    E.general = g.xyz != nullptr;
+    if (E.general) {
+#pragma unroll
+      for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) E.X[a][d] = g.xyz[d * g.nn + node[a]];
+      E.w = 0.0;
+    } else {
+      E.hx = g.hsz[e];
+      E.hy = g.hsz[g.ne + e];
+      E.hz = g.hsz[2 * g.ne + e];
+      E.w = 0.125 * (E.hx * E.hy * E.hz);
+    }
   } else {
+    E.general = false;
 #pragma unroll
     for (int a = 0; a < NL; ++a)
 #pragma unroll
@@ -108,8 +175,14 @@ __host__ __device__ constexpr int n_qp() { return NL == 8 ? 8 : 4; }
 template <int NL>
 __device__ __forceinline__ void elem_qp(int qi, const ElemG<NL>& E, QpT<NL>& Q) {
   if constexpr (NL == 8) {
-    qpoint(qi, gauss_offset(), E.hx, E.hy, E.hz, Q);
+    if (E.general) {
+      qpoint_general(qi, gauss_offset(), E.X, Q);
+    } else {
+      qpoint(qi, gauss_offset(), E.hx, E.hy, E.hz, Q);
+      Q.w = E.w;
+    }
   } else {
+    Q.w = E.w;
     const double ta = 0.58541019662496845446, tb = 0.13819660112501051518;
 #pragma unroll
     for (int a = 0; a < NL; ++a) {
@@ -181,7 +254,7 @@ __global__ void k_robin_elem(Geo g, const double* __restrict__ rho_n, double h, 
         }
         const double iface = sqrt(gx * gx + gy * gy + gz * gz);
         const double heff = h * pow(rq, p) * pow(1.0 - rq, q);
-        const double c = E.w * heff * iface;
+        const double c = Q.w * heff * iface;
         const double ct = c * t_env;
 #pragma unroll
         for (int a = 0; a < NL; ++a) {
@@ -261,14 +334,14 @@ k_hx_reduce(Geo g, const double* __restrict__ rho_n, const double* __restrict__ 
         gz += Q.gz[a] * r[a];
       }
       const double iface = sqrt(gx * gx + gy * gy + gz * gz);
-      den += E.w * iface;
+      den += Q.w * iface;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         if (j < L) {
           double tq = 0.0;
 #pragma unroll
           for (int a = 0; a < NL; ++a) tq += Q.N[a] * te[j][a];
-          num[j] += E.w * (-t_env * h * (tq - t_env) * iface);
+          num[j] += Q.w * (-t_env * h * (tq - t_env) * iface);
         }
       }
     }
@@ -311,7 +384,7 @@ __global__ void k_hx_adj_elem(Geo g, const double* __restrict__ rho_n, double h,
         gy += Q.gy[a] * r[a];
         gz += Q.gz[a] * r[a];
       }
-      const double c = E.w * (-t_env * hq * sqrt(gx * gx + gy * gy + gz * gz));
+      const double c = Q.w * (-t_env * hq * sqrt(gx * gx + gy * gy + gz * gz));
 #pragma unroll
       for (int a = 0; a < NL; ++a) f[a] += c * Q.N[a];
     }
@@ -360,8 +433,8 @@ __global__ void k_robin_grad_elem(Geo g, const double* __restrict__ rho_n,
       const double av = rp * sq;
       const double da = p * pow(rq, p - 1.0) * sq - q * rp * pow(1.0 - rq, q - 1.0);
       const double phi = 2.0 * t_env * tq - tq * tq;
-      const double c1 = E.w * h * da * iface * phi;
-      const double c2 = E.w * h * av * phi;
+      const double c1 = Q.w * h * da * iface * phi;
+      const double c2 = Q.w * h * av * phi;
       const double nx = gx / safe, ny = gy / safe, nz = gz / safe;
 #pragma unroll
       for (int a = 0; a < NL; ++a)
@@ -425,7 +498,7 @@ __global__ void k_grad_dot(Geo g, const double* __restrict__ X, const double* __
           ax += Q.gx[a] * xe[a]; ay += Q.gy[a] * xe[a]; az += Q.gz[a] * xe[a];
           bx += Q.gx[a] * ye[a]; by += Q.gy[a] * ye[a]; bz += Q.gz[a] * ye[a];
         }
-        s += E.w * (ax * bx + ay * by + az * bz);
+        s += Q.w * (ax * bx + ay * by + az * bz);
       }
       out[e * L + j] = s;
     }
@@ -448,12 +521,14 @@ struct topt_heat {
   int sm = 152;
   cudaStream_t stream = nullptr;
   DevBuf t, hsz, tg, tv, node_ptr, adj;
+  DevBuf xyz;                         // node coordinates of general hexahedra
   DevBuf surf_idx, surf;
   DevBuf fe, nodal;                   // element-vector and nodal scratch
   DevBuf partials, counter, out;      // k_hx_reduce
   int red_blocks = 0;
   topt::Geo geo() const {
-    return {t.as<int32_t>(), hsz.as<double>(), tg.as<double>(), tv.as<double>(), n_elem};
+    return {t.as<int32_t>(), hsz.as<double>(), tg.as<double>(), tv.as<double>(), n_elem,
+            xyz.p ? xyz.as<double>() : nullptr, n_nodes};
   }
   int grid(int64_t n) const { return topt::grid_for(n, topt::kHB, sm * 16); }
 };
@@ -478,26 +553,58 @@ int topt_heat_create_mesh(int64_t n_nodes, int64_t n_elem, int32_t nloc, const i
   for (int64_t i = 0; i < (int64_t)nloc * n_elem; ++i)
     if (t[i] < 0 || t[i] >= n_nodes) return fail(TOPT_BAD_INPUT, "heat_create: bad node index");
   std::vector<double> hs, tg, tv;
+  bool general = false;
   if (nloc == 8) {
-    // extents of every cell; the Robin kernels need axis-aligned boxes
+    // extents of every cell when all cells are axis-aligned boxes; any other
+    // hexahedron switches the handle to the general trilinear map (node
+    // coordinates on the device, Jacobian per Gauss point), whose Jacobian
+    // must be positive at every Gauss point
     hs.resize(3 * (size_t)n_elem);
-    for (int64_t e = 0; e < n_elem; ++e) {
+    for (int64_t e = 0; e < n_elem && !general; ++e) {
       int64_t nd[8];
       for (int a = 0; a < 8; ++a) nd[a] = t[(int64_t)a * n_elem + e];
       double lo[3], ext[3];
       for (int d = 0; d < 3; ++d) {
         lo[d] = p[d * n_nodes + nd[0]];
         ext[d] = p[d * n_nodes + nd[7]] - lo[d];
-        if (!(ext[d] > 0.0))
-          return fail(TOPT_BAD_INPUT, "heat_create: cell with non-positive extent");
+        if (!(ext[d] > 0.0)) general = true;
         hs[(size_t)d * n_elem + e] = ext[d];
       }
-      for (int a = 0; a < 8; ++a)
+      for (int a = 0; a < 8 && !general; ++a)
         for (int d = 0; d < 3; ++d) {
           const double want = lo[d] + (hex_off(a, d) ? ext[d] : 0.0);
-          if (std::fabs(p[d * n_nodes + nd[a]] - want) > 1e-9 * ext[d])
-            return fail(TOPT_BAD_INPUT, "heat_create: cells must be axis-aligned boxes");
+          if (std::fabs(p[d * n_nodes + nd[a]] - want) > 1e-9 * ext[d]) general = true;
         }
+    }
+    if (general) {
+      hs.clear();
+      const double G = 0.5 / std::sqrt(3.0);
+      for (int64_t e = 0; e < n_elem; ++e) {
+        double X[8][3];
+        for (int a = 0; a < 8; ++a)
+          for (int d = 0; d < 3; ++d) X[a][d] = p[d * n_nodes + t[(int64_t)a * n_elem + e]];
+        for (int q = 0; q < 8; ++q) {
+          const double xq[3] = {(q >> 2) & 1 ? 0.5 + G : 0.5 - G,
+                                (q >> 1) & 1 ? 0.5 + G : 0.5 - G, q & 1 ? 0.5 + G : 0.5 - G};
+          double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+          for (int a = 0; a < 8; ++a) {
+            double f[3], s3[3];
+            for (int k = 0; k < 3; ++k) {
+              f[k] = hex_off(a, k) ? xq[k] : 1.0 - xq[k];
+              s3[k] = hex_off(a, k) ? 1.0 : -1.0;
+            }
+            const double dr[3] = {s3[0] * f[1] * f[2], f[0] * s3[1] * f[2], f[0] * f[1] * s3[2]};
+            for (int d = 0; d < 3; ++d)
+              for (int k = 0; k < 3; ++k) J[d][k] += X[a][d] * dr[k];
+          }
+          const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) +
+                             J[0][1] * (J[1][2] * J[2][0] - J[1][0] * J[2][2]) +
+                             J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+          if (!(det > 0.0))
+            return fail(TOPT_BAD_INPUT,
+                        "heat_create: hexahedron with a non-positive Jacobian at a Gauss point");
+        }
+      }
     }
   } else {
     // P1 gradients: with J the columns x1 - x0, x2 - x0, x3 - x0, the
@@ -556,7 +663,9 @@ int topt_heat_create_mesh(int64_t n_nodes, int64_t n_elem, int32_t nloc, const i
   int rc;
   cudaStream_t s = nullptr;
   if ((rc = upload(h->t, t, (size_t)nt, s))) return rc;
-  if (nloc == 8) {
+  if (nloc == 8 && general) {
+    if ((rc = upload(h->xyz, p, 3 * (size_t)n_nodes, s))) return rc;
+  } else if (nloc == 8) {
     if ((rc = upload(h->hsz, hs.data(), hs.size(), s))) return rc;
   } else {
     if ((rc = upload(h->tg, tg.data(), tg.size(), s))) return rc;

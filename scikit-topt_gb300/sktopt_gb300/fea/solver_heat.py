@@ -30,7 +30,8 @@ Drop-in for ``FEM_SimpLinearHeatConduction`` (sktopt/fea/solver_heat.py:
 
 The volume integrals of the Robin and heat-exchange forms use the
 quadrature of a basis with intorder 2: the 2x2x2 Gauss rule on hexahedra
-(axis-aligned), the 4-point degree-2 rule on P1 tetrahedra.  Robin facets
+(boxes or the trilinear map of any hexahedron), the 4-point degree-2 rule on
+P1 tetrahedra; hexahedron faces take 2x2 Gauss on their bilinear map.  Robin facets
 are rows (element, axis, side) on hexahedra and (element, local face) on
 tetrahedra.  The nodal density average follows the reference's pairing of
 ``t.ravel()`` with ``np.repeat(rho, nloc)`` (node t[a, e] receives
@@ -64,12 +65,44 @@ def _tri_area(mesh, e, loc):
     return 0.5 * float(np.linalg.norm(np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0])))
 
 
+_G2 = 0.5 / np.sqrt(3.0)
+_FACE_PTS = [(0.5 - _G2, 0.5 - _G2), (0.5 - _G2, 0.5 + _G2), (0.5 + _G2, 0.5 - _G2),
+             (0.5 + _G2, 0.5 + _G2)]
+
+
+def _hex_face_rule(mesh, faces):
+    """2x2 Gauss rule on the bilinear map of every hexahedron face (rows
+    (element, axis, side)): the face's 4 local nodes (nf, 4), the shape values
+    at the 4 points (nf, 4 points, 4 nodes) and the weights times the area
+    element |dX/ds x dX/dt| (nf, 4).  Exact for the mass forms of planar
+    parallelogram faces (axis-aligned cells in particular)."""
+    faces = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+    nf = faces.shape[0]
+    loc = np.zeros((nf, 4), dtype=np.int64)
+    Nq = np.zeros((nf, 4, 4))
+    wq = np.zeros((nf, 4))
+    for k, (e, axis, side) in enumerate(faces):
+        ln = hex_face_local_nodes(int(axis), int(side))
+        ax = [d for d in range(3) if d != axis]
+        uv = HEX_OFFSETS[ln][:, ax]                                  # (4, 2) in {0, 1}
+        X = mesh.p[:, mesh.t[ln, e]]                                 # (3, 4)
+        loc[k] = ln
+        for q, (su, tv) in enumerate(_FACE_PTS):
+            fu = np.where(uv[:, 0] == 1, su, 1.0 - su)
+            fv = np.where(uv[:, 1] == 1, tv, 1.0 - tv)
+            du = np.where(uv[:, 0] == 1, 1.0, -1.0) * fv
+            dv = fu * np.where(uv[:, 1] == 1, 1.0, -1.0)
+            Nq[k, q] = fu * fv
+            wq[k, q] = 0.25 * np.linalg.norm(np.cross(X @ du, X @ dv))
+    return loc, Nq, wq
+
+
 def surface_robin_matrices(mesh, faces, h):
     """Per-face h * int N_a N_b over one element face (task_heat.py:
     106-134), in the owning element's local numbering.  Hexahedron faces
-    (rows (element, axis, side)): the tensor product of the two edge mass
-    matrices L/6 [[2, 1], [1, 2]]; tetrahedron faces (rows (element, local
-    face)): A/12 (1 + delta_ab).  Returns (n_faces, nloc^2)."""
+    (rows (element, axis, side)): 2x2 Gauss on the face's bilinear map (any
+    hexahedron); tetrahedron faces (rows (element, local face)): A/12 (1 +
+    delta_ab).  Returns (n_faces, nloc^2)."""
     if mesh.kind != "hex":
         out = np.zeros((len(faces), 4, 4))
         for k, (e, f) in enumerate(faces):
@@ -79,35 +112,30 @@ def surface_robin_matrices(mesh, faces, h):
                 for j, nj in enumerate(loc):
                     out[k, ni, nj] = h * a / 12.0 * (2.0 if i == j else 1.0)
         return out.reshape(len(faces), 16)
-    out = np.zeros((len(faces), 8, 8))
-    for k, (e, axis, side) in enumerate(faces):
-        loc = hex_face_local_nodes(int(axis), int(side))
-        ax = [d for d in range(3) if d != axis]
-        ext = mesh.p[:, mesh.t[7, e]] - mesh.p[:, mesh.t[0, e]]
-        a, b = ext[ax[0]], ext[ax[1]]
-        for i, ni in enumerate(loc):
-            for j, nj in enumerate(loc):
-                si, sj = HEX_OFFSETS[ni], HEX_OFFSETS[nj]
-                out[k, ni, nj] = h * (a / 6.0) * (1.0 + (si[ax[0]] == sj[ax[0]])) * \
-                    (b / 6.0) * (1.0 + (si[ax[1]] == sj[ax[1]]))
-    return out.reshape(len(faces), 64)
+    loc, Nq, wq = _hex_face_rule(mesh, faces)
+    m = h * np.einsum("kq,kqi,kqj->kij", wq, Nq, Nq)                 # (nf, 4, 4)
+    out = np.zeros((len(loc), 8, 8))
+    for i in range(4):
+        for j in range(4):
+            out[np.arange(len(loc)), loc[:, i], loc[:, j]] = m[:, i, j]
+    return out.reshape(len(loc), 64)
 
 
 def surface_robin_load(mesh, faces, h, t_env):
-    """h T_env int N_a over the faces (task_heat.py:121-135): a quarter of
-    the face area at each node of a hexahedron face, a third at each node of
-    a triangle."""
+    """h T_env int N_a over the faces (task_heat.py:121-135): 2x2 Gauss on
+    the bilinear map of a hexahedron face, a third of the area at each node
+    of a triangle."""
     f = np.zeros(mesh.nnodes)
     if mesh.kind != "hex":
         for e, fc in faces:
             loc = TET_FACES[int(fc)]
             np.add.at(f, mesh.t[loc, int(e)], h * t_env * _tri_area(mesh, int(e), loc) / 3.0)
         return f
-    for e, axis, side in faces:
-        loc = hex_face_local_nodes(int(axis), int(side))
-        ax = [d for d in range(3) if d != axis]
-        ext = mesh.p[:, mesh.t[7, e]] - mesh.p[:, mesh.t[0, e]]
-        np.add.at(f, mesh.t[loc, e], h * t_env * ext[ax[0]] * ext[ax[1]] / 4.0)
+    faces = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+    loc, Nq, wq = _hex_face_rule(mesh, faces)
+    fl = h * t_env * np.einsum("kq,kqi->ki", wq, Nq)                  # (nf, 4)
+    nodes = mesh.t[loc, faces[:, 0][:, None]]                        # (nf, 4)
+    np.add.at(f, nodes.ravel(), fl.ravel())
     return f
 
 

@@ -124,6 +124,22 @@ def create_box_hex(nx, ny, nz, hx=1.0, hy=1.0, hz=1.0) -> GridMesh:
                           np.arange(nz + 1) * float(hz))
 
 
+def create_box_hex_jittered(nx, ny, nz, lx, ly, lz, jitter=0.2, seed=0) -> GridMesh:
+    """Hex mesh of the nx x ny x nz grid on [0,lx]x[0,ly]x[0,lz] with every
+    interior node coordinate moved by U(-jitter*h, jitter*h) per axis
+    (``numpy.random.default_rng(seed)``); boundary coordinates stay on their
+    faces.  The cells are general trilinear hexahedra (the boundary faces
+    stay planar); the logical grid is kept for the multigrid hierarchy."""
+    m = structured_hex(np.linspace(0.0, lx, nx + 1), np.linspace(0.0, ly, ny + 1),
+                       np.linspace(0.0, lz, nz + 1))
+    ijk = m.node_ijk
+    d = np.random.default_rng(seed).uniform(-1.0, 1.0, size=m.p.shape)
+    h = np.array([lx / nx, ly / ny, lz / nz])[:, None]
+    inside = (ijk > 0) & (ijk < np.array([nx, ny, nz])[:, None])
+    p = m.p + np.where(inside, d * jitter * h, 0.0)
+    return GridMesh(p, m.t, "hex", m.shape, ijk, m.cell_of_elem)
+
+
 def create_box_hex_len(x_len, y_len, z_len, mesh_size) -> GridMesh:
     """sktopt/mesh/toy_problem.py:10-37."""
     n = [int(np.ceil(v / mesh_size)) for v in (x_len, y_len, z_len)]

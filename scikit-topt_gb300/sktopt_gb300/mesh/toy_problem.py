@@ -52,16 +52,21 @@ def heat_box(nx, ny, nz, patch=10, source=1.0, k=1.0):
 
 
 def heat_plate(nx=40, ny=40, nz=5, objective="compliance", avg_temp_weight=0.0,
-               dirichlet_values=600.0, robin=True):
+               dirichlet_values=600.0, robin=True, jitter=0.0, seed=0):
     """The heat task of sktopt's tests/test_global_flow.py:53-104 on an
     nx x ny x nz grid: 8 x 8 x 1 plate (the reference meshes it at 0.2, i.e.
     40 x 40 x 5), Robin h = 4e-5, T_env = 300 on x = 0 and y = 8, T = 600 on
     the boundary facets with midpoints in [7.6, 8] x [0, 0.4] x [0, 1],
-    k = 10, every element designable (design_robin_boundary=True)."""
-    from .grid import get_points_in_range as rng, structured_hex
+    k = 10, every element designable (design_robin_boundary=True).  With
+    jitter > 0 the interior nodes move by U(-jitter h, jitter h) (seeded):
+    general hexahedra with the same boundary faces."""
+    from .grid import create_box_hex_jittered, get_points_in_range as rng, structured_hex
     lx, ly, lz = 8.0, 8.0, 1.0
-    mesh = structured_hex(np.linspace(0, lx, nx + 1), np.linspace(0, ly, ny + 1),
-                          np.linspace(0, lz, nz + 1))
+    if jitter > 0.0:
+        mesh = create_box_hex_jittered(nx, ny, nz, lx, ly, lz, jitter=jitter, seed=seed)
+    else:
+        mesh = structured_hex(np.linspace(0, lx, nx + 1), np.linspace(0, ly, ny + 1),
+                              np.linspace(0, lz, nz + 1))
     return LinearHeatConduction.from_boundaries(
         mesh, rng((lx - lx / 20, lx), (0.0, ly / 20), (0.0, lz)), dirichlet_values,
         [rng((0.0, 0.0), (0.0, ly), (0.0, lz)), rng((0.0, lx), (ly, ly), (0.0, lz))]

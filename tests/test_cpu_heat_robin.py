@@ -15,7 +15,11 @@
 * the plate task's Dirichlet nodes and Robin facets match the oracle's;
 * the oracle reproduces its committed golden fixtures (heat plate objectives,
   adjoints, energies, sensitivities; tet traction loads, also against the
-  product's host-side traction assembly).
+  product's host-side traction assembly);
+* on P1 tetrahedra and on general (jittered) hexahedra: the quadrature's
+  volume and linear-field identities, surface sums and the product's surface
+  matrices, the explicit gradient by central differences, and (hexahedra)
+  the per-element conduction matrices of the oracle against the product's.
 """
 import numpy as np
 import pytest
@@ -261,6 +265,85 @@ def test_tet_surface_robin_sums_and_product_match():
 def test_tet_explicit_robin_gradient_finite_differences():
     t, m = _tet_plate((4, 4, 2))
     Q = hr.tet_quadrature(m)
+    rng = np.random.default_rng(8)
+    rho_n = rng.uniform(0.2, 0.8, m.nnodes)
+    T = rng.uniform(250.0, 650.0, m.nnodes)
+    h, te, p, q = 4e-5, 300.0, 3.0, 4.0
+    N, dN, wd = Q
+
+    def G(r):
+        rq, g = hr._at_qp(N, dN, m, r)
+        tq, _ = hr._at_qp(N, dN, m, T)
+        iface = np.sqrt(np.sum(g ** 2, axis=2))
+        return float(np.sum(wd * h * rq ** p * (1 - rq) ** q * iface * (2 * te * tq - tq * tq)))
+
+    grad = hr.robin_explicit_grad(m, Q, rho_n, T, h, te, p, q)
+    for n in rng.choice(m.nnodes, 6, replace=False):
+        e = np.zeros(m.nnodes)
+        e[n] = 1e-6
+        fd = (G(rho_n + e) - G(rho_n - e)) / 2e-6
+        assert abs(fd - grad[n]) <= 1e-6 * max(abs(grad).max(), 1e-300), (n, fd, grad[n])
+
+
+# --- general (non-box) hexahedra ---------------------------------------------
+def _jit_plate(n=(6, 6, 2), objective="compliance", avg_w=0.0):
+    from oracle import mesh as omesh
+    from sktopt_gb300.mesh import toy_problem
+    t = toy_problem.heat_plate(*n, objective=objective, avg_temp_weight=avg_w, jitter=0.2,
+                               seed=3)
+    m = omesh.GridMesh(t.mesh.p, t.mesh.t, "hex", None, None, None)
+    return t, m
+
+
+def test_general_hex_mesh_is_not_boxes_and_keeps_the_boundary():
+    from sktopt_gb300.mesh import toy_problem
+    t, m = _jit_plate()
+    assert not ofem._is_uniform_box(m)
+    box = toy_problem.heat_plate(6, 6, 2).mesh.p
+    # interior nodes moved by up to 0.2 h per axis, boundary coordinates kept
+    assert 0.1 < np.abs(m.p - box).max() <= 0.2 * 8.0 / 6.0 + 1e-12
+    for d, top in enumerate((8.0, 8.0, 1.0)):
+        on = np.isclose(box[d], 0.0) | np.isclose(box[d], top)
+        np.testing.assert_array_equal(m.p[d, on], box[d, on])
+
+
+def test_general_hex_quadrature_exact_on_linear_fields():
+    """2x2x2 Gauss on the trilinear map: detJ is of degree <= 2 per
+    direction, so the weights sum to the plate's volume and |grad rho| of a
+    linear nodal field (reproduced exactly by the trilinear element)
+    integrates to |a| x volume; the per-element conduction matrices of the
+    oracle and of the product's host code agree."""
+    from sktopt_gb300.fea import composer
+    t, m = _jit_plate()
+    Q = hr.hex_quadrature(m)
+    assert abs(Q[2].sum() - 64.0) <= 1e-12 * 64.0
+    a = np.array([0.3, -0.2, 0.5])
+    rho_n = 0.1 + a @ m.p * 0.01
+    den = hr.hx_den(m, Q, rho_n)
+    assert abs(den - 0.01 * np.linalg.norm(a) * 64.0) <= 1e-12 * den
+    _, Kh_o, _ = ofem.element_matrices(m, 0.3)
+    _, Kh_p, _ = composer.element_matrices(t.mesh, 0.3)
+    assert Kh_p.ndim == 3
+    np.testing.assert_allclose(Kh_p, Kh_o, rtol=0, atol=1e-12 * np.abs(Kh_o).max())
+
+
+def test_general_hex_surface_robin_sums_and_product_match():
+    from sktopt_gb300.fea.solver_heat import surface_robin_load, surface_robin_matrices
+    t, m = _jit_plate((5, 4, 3))
+    for faces, area in zip(t.robin_groups, (8.0 * 1.0, 8.0 * 1.0)):
+        faces = np.asarray(faces)
+        Me, load = hr.surface_robin(m, faces, 2.0, 300.0)
+        assert abs(Me.sum() - 2.0 * area) <= 1e-12 * area
+        assert abs(load.sum() - 2.0 * 300.0 * area) <= 1e-10 * area
+        np.testing.assert_allclose(surface_robin_matrices(t.mesh, faces, 2.0).reshape(-1, 8, 8),
+                                   Me, rtol=1e-13, atol=1e-20)
+        np.testing.assert_allclose(surface_robin_load(t.mesh, faces, 2.0, 300.0), load,
+                                   rtol=1e-13, atol=1e-18)
+
+
+def test_general_hex_explicit_robin_gradient_finite_differences():
+    t, m = _jit_plate((4, 4, 2))
+    Q = hr.hex_quadrature(m)
     rng = np.random.default_rng(8)
     rho_n = rng.uniform(0.2, 0.8, m.nnodes)
     T = rng.uniform(250.0, 650.0, m.nnodes)

@@ -216,3 +216,47 @@ def test_heat_robin_tetrahedra_match_oracle(native_lib, objective, avg_w, precis
         assert _rel(fem.lam.cpu().numpy(), pb.lam) <= vtol
     assert _rel(fem.energy_multi_load(rho, p, u), en_ref) <= vtol
     assert _rel(fem.compliance_sensitivity_multi_load(rho, p, u), dc_ref) <= vtol
+
+
+def _jit_pair(n, objective, avg_w):
+    from oracle import mesh as omesh
+    from sktopt_gb300.mesh import toy_problem
+    tsk = toy_problem.heat_plate(*n, objective=objective, avg_temp_weight=avg_w, jitter=0.2,
+                                 seed=5)
+    m = omesh.GridMesh(tsk.mesh.p, tsk.mesh.t, "hex", None, None, None)
+    pb = hr.HeatRobinProblem(m, np.unique(np.asarray(tsk.dirichlet_nodes)), 600.0, k0=10.0,
+                             robin_faces=[np.asarray(g) for g in tsk.robin_groups],
+                             robin_coefficient=4.0e-5, robin_bc_value=300.0,
+                             objective=objective, avg_temp_weight=avg_w)
+    return tsk, m, pb
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("objective,avg_w", [("compliance", 0.0), ("heat_exchange", 0.5),
+                                             ("averaged_temp", 0.0)])
+def test_heat_robin_general_hexahedra_match_oracle(native_lib, objective, avg_w, precision):
+    """The plate with its interior nodes jittered (general trilinear
+    hexahedra, planar boundary faces): virtual Robin, heat-exchange and
+    gradient forms with the Jacobian at every Gauss point, surface Robin
+    terms on the faces' bilinear maps, against the oracle (same tolerances
+    as the box plate)."""
+    tsk, m, pb = _jit_pair((10, 10, 2), objective, avg_w)
+    rho = np.random.default_rng(23).uniform(0.1, 1.0, m.nelements)
+    p, kmin = 3.0, 10.0 * 1e-3
+    J_ref, T_ref = pb.objectives(rho, p, kmin)
+    en_ref = pb.energy(rho, p, kmin, T_ref)
+    dc_ref = pb.custom_sensitivity(rho, p, kmin, T_ref)
+    fem = _fem(tsk, precision)
+    u = np.zeros((tsk.n_dof, 1))
+    J = fem.objectives_multi_load(rho, p, u)
+    K, _, _ = pb.operator(rho, p, kmin)
+    aT = np.abs(T_ref[:, 0])
+    floor = 4 * np.finfo(float).eps * (aT @ (abs(K) @ aT))
+    tol = (1e-9 if objective == "heat_exchange" else 1e-10) if precision == "fp64" else 1e-6
+    assert abs(J[0] - J_ref[0]) <= tol * abs(J_ref[0]) + floor, (J, J_ref, floor)
+    np.testing.assert_allclose(u, T_ref, rtol=0, atol=1e-8 * np.abs(T_ref).max())
+    vtol = 1e-8 if precision == "fp64" else 1e-5
+    if objective != "compliance":
+        assert _rel(fem.lam.cpu().numpy(), pb.lam) <= vtol
+    assert _rel(fem.energy_multi_load(rho, p, u), en_ref) <= vtol
+    assert _rel(fem.compliance_sensitivity_multi_load(rho, p, u), dc_ref) <= vtol
