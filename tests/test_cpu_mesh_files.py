@@ -1,9 +1,11 @@
 """Mesh files, boundary facets and surface tractions (CPU).
 
-* gmsh MSH 2.2 round trip (hexahedra and jittered tetrahedra): nodes,
-  connectivity, named boundaries and subdomains come back unchanged;
+* gmsh MSH 2.2 and 4.1 round trips, ASCII and binary (little- and
+  big-endian), hexahedra and jittered tetrahedra: nodes, connectivity,
+  named boundaries and subdomains come back unchanged;
 * a hand-written MSH 4.1 file (two hexahedra, entity-level physical groups)
-  parses to the MeshHex local order with the expected facets;
+  parses to the MeshHex local order with the expected facets, and so do its
+  binary MSH 4.1 and MSH 2.2 forms packed field by field with ``struct``;
 * boundary facets and traction loads (task_elastic.py:15-81) against the
   oracle restatement (other quadrature rules): 1e-13 relative;
 * ``from_mesh_tags`` (task_elastic.py:266-317, task_heat.py:252-321) builds
@@ -48,15 +50,22 @@ def test_boundary_facets_and_tractions_match_oracle(k):
 
 
 @pytest.mark.parametrize("k", [0, 1])
-def test_msh22_round_trip(tmp_path, k):
+@pytest.mark.parametrize("version,binary,order", [("2.2", False, "<"), ("2.2", True, "<"),
+                                                  ("2.2", True, ">"), ("4.1", False, "<"),
+                                                  ("4.1", True, "<"), ("4.1", True, ">")])
+def test_msh_round_trip(tmp_path, k, version, binary, order):
     from sktopt_gb300.mesh import boundary_facets, read_msh, write_msh
     from sktopt_gb300.mesh import get_points_in_range as rng
     m = _meshes()[k]
     b = {"dirichlet": boundary_facets(m, rng((0, 0), (0, 9), (0, 9))),
          "neumann_1": boundary_facets(m, rng((m.p[0].max(), 9), (0, 9), (0, 9)))}
-    sub = {"design": np.arange(m.nelements)[::2], "solid": np.arange(m.nelements)[1::2]}
+    # overlapping subdomains: an element in two groups
+    sub = {"design": np.arange(m.nelements)[::2], "solid": np.arange(m.nelements)[1::2],
+           "probe": np.arange(m.nelements)[:3]}
     path = tmp_path / "m.msh"
-    write_msh(path, m, boundaries=b, subdomains=sub)
+    write_msh(path, m, boundaries=b, subdomains=sub, version=version, binary=binary,
+              byteorder=order)
+    assert (b"\x00" in path.read_bytes()) == binary
     r = read_msh(path)
     assert r.kind == m.kind and not r.has_grid
     assert np.array_equal(r.t, m.t) and np.array_equal(r.p, m.p)
@@ -98,6 +107,85 @@ $Elements
 4 {h1}
 $EndElements
 """
+
+
+def _two_hex_data():
+    nid = lambda x, y, z: 1 + x + 3 * y + 6 * z          # noqa: E731
+    xyz = [(x, y, z) for z in range(2) for y in range(2) for x in range(3)]
+    gm = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    hexes = [[nid(x + o[0], o[1], o[2]) for o in gm] for x in (0, 1)]
+    quads = [[nid(x, y, z) for y, z in ((0, 0), (1, 0), (1, 1), (0, 1))] for x in (0, 2)]
+    return nid, xyz, hexes, quads
+
+
+def _check_two_hex(m):
+    assert m.kind == "hex" and m.nelements == 2 and m.nnodes == 12
+    for e in range(2):
+        for a, o in enumerate(omesh.HEX_OFFSETS):
+            assert np.array_equal(m.p[:, m.t[a, e]], [e + o[0], o[1], o[2]])
+    assert np.array_equal(m.boundaries["dirichlet"], [[0, 0]])
+    assert np.array_equal(m.boundaries["neumann"], [[1, 1]])
+    assert np.array_equal(m.subdomains["design"], [0, 1])
+
+
+_NAMES = b'''$PhysicalNames
+3
+2 1 "dirichlet"
+2 2 "neumann"
+3 3 "design"
+$EndPhysicalNames
+'''
+
+
+@pytest.mark.parametrize("order", ["<", ">"])
+def test_msh41_binary_packed_by_hand(tmp_path, order):
+    """The two-hexahedra file in binary MSH 4.1, each field packed with
+    struct as the format lays it out: size_t counts and tags, int entity
+    dimensions / tags / types, double coordinates and bounding boxes."""
+    import struct
+    nid, xyz, hexes, quads = _two_hex_data()
+    o = order
+    ent = struct.pack(o + "4Q", 0, 0, 2, 1)
+    for tag, ph in ((1, 1), (2, 2)):
+        ent += struct.pack(o + "i6dQiQ", tag, 0, 0, 0, 2, 1, 1, 1, ph, 0)
+    ent += struct.pack(o + "i6dQiQ", 1, 0, 0, 0, 2, 1, 1, 1, 3, 0)
+    nodes = struct.pack(o + "4Q", 1, 12, 1, 12) + struct.pack(o + "3iQ", 3, 1, 0, 12)
+    nodes += struct.pack(o + "12Q", *[nid(*c) for c in xyz])
+    nodes += struct.pack(o + "36d", *[float(v) for c in xyz for v in c])
+    els = struct.pack(o + "4Q", 3, 4, 1, 4)
+    els += struct.pack(o + "3iQ", 2, 1, 3, 1) + struct.pack(o + "5Q", 1, *quads[0])
+    els += struct.pack(o + "3iQ", 2, 2, 3, 1) + struct.pack(o + "5Q", 2, *quads[1])
+    els += struct.pack(o + "3iQ", 3, 1, 5, 2) + struct.pack(o + "9Q", 3, *hexes[0])
+    els += struct.pack(o + "9Q", 4, *hexes[1])
+    data = (b"$MeshFormat\n4.1 1 8\n" + struct.pack(o + "i", 1) + b"\n$EndMeshFormat\n" +
+            _NAMES + b"$Entities\n" + ent + b"\n$EndEntities\n$Nodes\n" + nodes +
+            b"\n$EndNodes\n$Elements\n" + els + b"\n$EndElements\n")
+    from sktopt_gb300.mesh import read_msh
+    (tmp_path / "b41.msh").write_bytes(data)
+    _check_two_hex(read_msh(tmp_path / "b41.msh"))
+
+
+@pytest.mark.parametrize("order", ["<", ">"])
+def test_msh22_binary_packed_by_hand(tmp_path, order):
+    """The same mesh in binary MSH 2.2: nodes as (int tag, 3 doubles), the
+    elements in blocks headed by (type, count, number of tags), each element
+    (int number, int tags, int nodes); a point element (type 15) to step
+    over."""
+    import struct
+    nid, xyz, hexes, quads = _two_hex_data()
+    o = order
+    nodes = b"".join(struct.pack(o + "i3d", nid(*c), *[float(v) for v in c]) for c in xyz)
+    els = struct.pack(o + "3i", 15, 1, 2) + struct.pack(o + "4i", 1, 0, 0, 1)
+    els += struct.pack(o + "3i", 3, 2, 2)
+    els += struct.pack(o + "7i", 2, 1, 1, *quads[0]) + struct.pack(o + "7i", 3, 2, 2, *quads[1])
+    els += struct.pack(o + "3i", 5, 2, 2)
+    els += struct.pack(o + "11i", 4, 3, 3, *hexes[0]) + struct.pack(o + "11i", 5, 3, 3, *hexes[1])
+    data = (b"$MeshFormat\n2.2 1 8\n" + struct.pack(o + "i", 1) + b"\n$EndMeshFormat\n" +
+            _NAMES + b"$Nodes\n12\n" + nodes + b"\n$EndNodes\n$Elements\n5\n" + els +
+            b"\n$EndElements\n")
+    from sktopt_gb300.mesh import read_msh
+    (tmp_path / "b22.msh").write_bytes(data)
+    _check_two_hex(read_msh(tmp_path / "b22.msh"))
 
 
 def test_msh41_two_hexahedra(tmp_path):
@@ -173,9 +261,14 @@ def test_heat_from_mesh_tags_matches_plate(tmp_path):
 
 def test_msh_rejects_unsupported_input(tmp_path):
     from sktopt_gb300.mesh import read_msh
+    # binary without its endianness mark, and a truncated binary node block
     (tmp_path / "bin.msh").write_text("$MeshFormat\n4.1 1 8\n$EndMeshFormat\n")
-    with pytest.raises(ValueError, match="binary"):
+    with pytest.raises(ValueError, match="endianness"):
         read_msh(tmp_path / "bin.msh")
+    (tmp_path / "trunc.msh").write_bytes(b"$MeshFormat\n2.2 1 8\n\x01\x00\x00\x00\n"
+                                         b"$EndMeshFormat\n$Nodes\n5\n\x01\x00")
+    with pytest.raises(ValueError, match="truncated"):
+        read_msh(tmp_path / "trunc.msh")
     (tmp_path / "none.msh").write_text("hello\n")
     with pytest.raises(ValueError, match="not a gmsh"):
         read_msh(tmp_path / "none.msh")
