@@ -163,6 +163,18 @@ def test_msh41_binary_packed_by_hand(tmp_path, order):
     from sktopt_gb300.mesh import read_msh
     (tmp_path / "b41.msh").write_bytes(data)
     _check_two_hex(read_msh(tmp_path / "b41.msh"))
+    # an unknown section and a point-element block (type 15) are stepped over
+    pts = struct.pack(o + "3iQ", 0, 1, 15, 1) + struct.pack(o + "2Q", 9, 1)
+    els2 = struct.pack(o + "4Q", 4, 5, 1, 9) + els[32:] + pts
+    data2 = data.replace(els, els2).replace(
+        b"$Entities", b"$Comments\nwritten by hand\n$EndComments\n$Entities")
+    (tmp_path / "b41x.msh").write_bytes(data2)
+    _check_two_hex(read_msh(tmp_path / "b41x.msh"))
+    # an element type this reader does not know
+    bad = data.replace(struct.pack(o + "3iQ", 3, 1, 5, 2), struct.pack(o + "3iQ", 3, 1, 99, 2))
+    (tmp_path / "b41bad.msh").write_bytes(bad)
+    with pytest.raises(ValueError, match="element type 99"):
+        read_msh(tmp_path / "b41bad.msh")
 
 
 @pytest.mark.parametrize("order", ["<", ">"])
