@@ -218,11 +218,16 @@ def test_heat_robin_tetrahedra_match_oracle(native_lib, objective, avg_w, precis
     assert _rel(fem.compliance_sensitivity_multi_load(rho, p, u), dc_ref) <= vtol
 
 
-def _jit_pair(n, objective, avg_w):
+def _jit_pair(n, objective, avg_w, drop_grid=False):
+    import dataclasses
     from oracle import mesh as omesh
     from sktopt_gb300.mesh import toy_problem
+    from sktopt_gb300.mesh.grid import GridMesh
     tsk = toy_problem.heat_plate(*n, objective=objective, avg_temp_weight=avg_w, jitter=0.2,
                                  seed=5)
+    if drop_grid:
+        tsk = dataclasses.replace(tsk, mesh=GridMesh(tsk.mesh.p, tsk.mesh.t, "hex"))
+        assert not tsk.mesh.has_grid
     m = omesh.GridMesh(tsk.mesh.p, tsk.mesh.t, "hex", None, None, None)
     pb = hr.HeatRobinProblem(m, np.unique(np.asarray(tsk.dirichlet_nodes)), 600.0, k0=10.0,
                              robin_faces=[np.asarray(g) for g in tsk.robin_groups],
@@ -232,15 +237,20 @@ def _jit_pair(n, objective, avg_w):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-@pytest.mark.parametrize("objective,avg_w", [("compliance", 0.0), ("heat_exchange", 0.5),
-                                             ("averaged_temp", 0.0)])
-def test_heat_robin_general_hexahedra_match_oracle(native_lib, objective, avg_w, precision):
+@pytest.mark.parametrize("objective,avg_w,drop_grid", [("compliance", 0.0, False),
+                                                       ("heat_exchange", 0.5, False),
+                                                       ("averaged_temp", 0.0, False),
+                                                       ("heat_exchange", 0.5, True)])
+def test_heat_robin_general_hexahedra_match_oracle(native_lib, objective, avg_w, drop_grid,
+                                                   precision):
     """The plate with its interior nodes jittered (general trilinear
     hexahedra, planar boundary faces): virtual Robin, heat-exchange and
     gradient forms with the Jacobian at every Gauss point, surface Robin
     terms on the faces' bilinear maps, against the oracle (same tolerances
-    as the box plate)."""
-    tsk, m, pb = _jit_pair((10, 10, 2), objective, avg_w)
+    as the box plate).  drop_grid: the same mesh without its logical grid,
+    as read from a file, solved on the scalar smoothed-aggregation
+    hierarchy."""
+    tsk, m, pb = _jit_pair((10, 10, 2), objective, avg_w, drop_grid)
     rho = np.random.default_rng(23).uniform(0.1, 1.0, m.nelements)
     p, kmin = 3.0, 10.0 * 1e-3
     J_ref, T_ref = pb.objectives(rho, p, kmin)

@@ -38,8 +38,11 @@ def test_percentile_matches_numpy(native_lib, n, q):
     assert got == pytest.approx(ref, rel=1e-15, abs=0.0)
 
 
-@pytest.mark.parametrize("kind", ["hex", "tet"])
+@pytest.mark.parametrize("kind", ["hex", "tet", "tet_no_grid"])
 def test_helmholtz_filter_matches_oracle(native_lib, kind):
+    """tet_no_grid: the jittered tets with the logical grid dropped, as a
+    mesh read from a file -- the nodal Helmholtz solves then run on the
+    scalar (bs = 1) smoothed-aggregation hierarchy built on the GPU."""
     import torch
     from sktopt_gb300.filters import HelmholtzFilterNodal
     from sktopt_gb300.mesh import grid
@@ -51,6 +54,9 @@ def test_helmholtz_filter_matches_oracle(native_lib, kind):
         m = grid.create_box_tet(6, 4, 3, 1.5, 1.0, 0.75, jitter=0.2, seed=4)
         om = omesh.create_box_tet(6, 4, 3, 1.5, 1.0, 0.75, jitter=0.2, seed=4)
         r = 0.2
+        if kind == "tet_no_grid":
+            m = grid.GridMesh(m.p, m.t, "tet")
+            assert not m.has_grid
     vol = omesh.elements_volume(om)
     mask = np.ones(m.nelements, bool)
     mask[:: 9] = False
